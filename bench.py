@@ -1,0 +1,400 @@
+"""Benchmark: simwave forward propagation on one GB300.
+
+Workload (default): 3D variable-density acoustic forward, 384^3 float32
+model at 12.5 m (472^3 extended grid: 40-point damping layer of degree 3 and
+alpha 0.001, order-8 halo), velocity 1500 + 3000 smoothstep(depth) with seeded
+Gaussian-smoothed noise (sigma 8 points, +-10 %) clipped to [1500, 4500] m/s,
+Gardner density 310 v^0.25, boundary 'none', tf 1.5 s (T = 1201 CFL steps),
+15 Hz Ricker at the surface centre, 128 x 128 receiver carpet at 10 m depth,
+saving stride 50 (25 snapshots). Synthetic, seeded inputs.
+
+One "step" is one complete forward run (all T time steps) of that shot.
+Metric: grid-point updates per second (interior points x time steps) in
+Gpts/s, whole job over all ranks.
+
+  value       device-resident inputs (simwave_forward_device), CUDA events on
+              the launching stream around each run
+  e2e         the reference-facing C ABI (the drop-in `forward` the
+              Middleware calls) with host numpy buffers; host<->device copies
+              inside the timed region
+  roofline    stencil kernel: algorithmic bytes per launch (20 B per interior
+              point: read u_cur, u_prev, velocity, density, write u_next) over
+              its mean launch time (CUDA events on the same stream)
+  cpu_baseline the CPU checker (C restatement, OpenMP, all host cores) on a
+              bounded sample of the same workload (fewer time steps)
+
+`--impl reference` times the reference's CPU algorithm (the C restatement)
+on the host cores instead and prints the same metric.
+Multi-GPU (torchrun): independent replicas, one shot per rank, no collective
+on the data path.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gpts/s (grid-point updates/s) and HBM GB/s vs roofline, 3D VD so8 forward"
+BYTES_PER_UPDATE = {False: 16, True: 20}  # float32, constant / variable density
+
+_MODEL_CACHE = {}
+
+
+def _smooth_noise(shape, sigma, seed):
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    g = gaussian_filter(rng.standard_normal(shape).astype(np.float32), sigma,
+                        mode="wrap")
+    return g / np.abs(g).max()
+
+
+def config2_model(n=384):
+    if n in _MODEL_CACHE:
+        return _MODEL_CACHE[n]
+    z = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    smooth = 3 * z ** 2 - 2 * z ** 3
+    base = 1500.0 + 3000.0 * smooth
+    noise = _smooth_noise((n, n, n), 8.0, seed=2024)
+    vel = base[:, None, None] * (1.0 + 0.1 * noise)
+    vel = np.clip(vel, 1500.0, 4500.0).astype(np.float32)
+    den = (310.0 * vel ** 0.25).astype(np.float32)
+    _MODEL_CACHE[n] = (vel, den)
+    return vel, den
+
+
+def config2_arguments(timesteps=None, n=384, stride=50):
+    """Middleware keyword arguments of the 3D benchmark shot.
+
+    ``timesteps`` truncates the run (same dt and wavelet samples) for tests
+    and bounded CPU samples."""
+    import simwave_gb300 as sw
+    vel, den = config2_model(n)
+    h = 12.5
+    top = (n - 1) * h
+    sm = sw.SpaceModel((0, top, 0, top, 0, top), (h, h, h), vel, den,
+                       space_order=8, dtype=np.float32)
+    sm.config_boundary(damping_length=40 * h, boundary_condition="none",
+                       damping_polynomial_degree=3, damping_alpha=0.001)
+    tm = sw.TimeModel(space_model=sm, tf=1.5, saving_stride=stride)
+    centre = top / 2
+    src = sw.Source(sm, coordinates=[(0.0, centre, centre)], window_radius=4)
+    g = (np.arange(128) + 0.5) * (top / 128)
+    gx, gy = np.meshgrid(g, g, indexing="ij")
+    carpet = np.stack([np.full(gx.size, 10.0), gx.ravel(), gy.ravel()], axis=1)
+    rec = sw.Receiver(sm, coordinates=carpet, window_radius=4)
+    solver = sw.Solver(sm, tm, src, rec, sw.RickerWavelet(15.0, tm))
+    kw = solver.forward_arguments()
+    if timesteps is not None and timesteps < kw["end_timestep"]:
+        T = int(timesteps)
+        kw["end_timestep"] = T
+        kw["wavelet"] = np.ascontiguousarray(kw["wavelet"][:T])
+        kw["wavelet_size"] = T
+        kw["shot_record"] = np.zeros((T, kw["num_receivers"]), np.float32)
+        nsnap = 1 if stride == 0 else len(range(0, T, stride))
+        kw["num_snapshots"] = nsnap + 2
+        kw["u_full"] = np.zeros((nsnap + 2,) + kw["u_full"].shape[1:],
+                                np.float32)
+    return kw
+
+
+def interior_updates(kw):
+    shape = kw["velocity_model"].shape
+    r = kw["space_order"] // 2
+    pts = 1
+    for n in shape:
+        pts *= n - 2 * r
+    T = kw["end_timestep"] - kw["begin_timestep"] + 1
+    return pts, pts * T
+
+
+# ---------------------------------------------------------------------------
+# clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU checker timing (bounded sample)
+
+def cpu_sample(steps, threads=None):
+    """Gpts/s of the C restatement on `steps` time steps of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = threads or os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    kw = config2_arguments(timesteps=steps, stride=0)
+    pts, updates = interior_updates(kw)
+    _, _, secs = oracle.forward("port", x_stride="layout", **kw)
+    return updates / secs / 1e9, secs, threads
+
+
+# ---------------------------------------------------------------------------
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference_arm(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps_t = args.cpu_steps
+    for _ in range(args.warmup):
+        cpu_sample(max(2, steps_t // 4))
+    rates, total = [], 0.0
+    threads = os.cpu_count()
+    for _ in range(args.steps):
+        rate, secs, threads = cpu_sample(steps_t)
+        rates.append(rate)
+        total += secs
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4),
+        "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "3d_vd_so8_472cube_T1201_s50",
+                   "sample": "%d of 1201 time steps per step" % steps_t,
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Gpts/s",
+                         "cores": threads, "kind": "port",
+                         "sample": "%d time steps of the 472^3 grid, OpenMP"
+                                   % steps_t},
+        "e2e": {"value": round(value, 4), "unit": "Gpts/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--timesteps", type=int, default=None,
+                    help="truncate the shot (default: full T = 1201)")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=12)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    world, rank, local = dist_setup(args.gpus)
+    import torch
+    from simwave_gb300.backend import _lib
+    from simwave_gb300.backend.middleware import Middleware
+    from simwave_gb300.device import DeviceProblem
+
+    torch.cuda.set_device(local)
+    kw = config2_arguments(timesteps=args.timesteps)
+    pts, updates = interior_updates(kw)
+    dp = DeviceProblem(kw, device="cuda:%d" % local)
+    stream = torch.cuda.current_stream()
+
+    # warm-up runs
+    for _ in range(args.warmup):
+        dp.reset()
+        dp.run(stream)
+    torch.cuda.synchronize()
+
+    # resident timing: CUDA events around each full forward on its stream
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ms = []
+    launches = 0
+    for _ in range(args.steps):
+        dp.reset()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = dp.run(stream)
+        e1.record(stream)
+        launches += st["kernel_launches"]
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    clock_info = clocks.stop()
+    total_ms = max_over_ranks(float(np.sum(ms)), world)
+    ms_per_step = total_ms / args.steps
+    value = updates * world / (ms_per_step / 1e3) / 1e9
+
+    # stencil kernel time: events around each stencil launch, same stream
+    dp.reset()
+    st = dp.run(stream, time_kernels=True)
+    stencil_ms = st["stencil_ms"] / max(st["stencil_launches"], 1)
+    vd = "density_model" in kw and kw["density_model"] is not None
+    bytes_per_launch = pts * BYTES_PER_UPDATE[vd]
+    achieved = bytes_per_launch / (stencil_ms / 1e3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "stencil_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            t = json.load(f)
+        traffic = t.get("bytes_per_launch_full_size")
+    del dp
+    torch.cuda.empty_cache()
+
+    # end-to-end through the reference-facing C ABI with host buffers
+    e2e_ms, h2d, d2h = [], 0, 0
+    mw = Middleware()
+    import contextlib
+    import io
+    for i in range(args.e2e_steps + 1):
+        k = dict(kw)
+        k["u_full"] = np.zeros_like(kw["u_full"])
+        k["shot_record"] = np.zeros_like(kw["shot_record"])
+        barrier(world)
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(io.StringIO()):
+            mw.exec("forward", **k)
+        t1 = time.perf_counter()
+        if i > 0:  # first call allocates the library's device buffers
+            e2e_ms.append(1000 * (t1 - t0))
+            s = _lib.last_stats()
+            h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+            launches_e2e = s["kernel_launches"]
+    e2e_total = max_over_ranks(float(np.sum(e2e_ms)), world)
+    e2e_value = updates * world / (e2e_total / len(e2e_ms) / 1e3) / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, secs, threads = cpu_sample(args.cpu_steps)
+        cpu = {"value": round(rate, 4), "unit": "Gpts/s", "cores": threads,
+               "kind": "port",
+               "sample": "%d of 1201 time steps on the full 472^3 grid "
+                         "(C restatement, OpenMP, %.1f s)" % (args.cpu_steps, secs)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Gpts/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "3d_vd_so8_472cube_T%d_s50" % kw["end_timestep"],
+                       "grid": list(kw["velocity_model"].shape),
+                       "timesteps": kw["end_timestep"],
+                       "updates_per_step": updates,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (11.4 GB wavefield slots)"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": peak_src,
+                         "kernel_ms": round(stencil_ms, 4),
+                         "bytes_per_launch": bytes_per_launch},
+            "e2e": {"value": round(e2e_value, 3), "unit": "Gpts/s",
+                    "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": round(e2e_total / len(e2e_ms), 3)},
+            "gpu_launches": int(launches),
+            "clocks": clock_info,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

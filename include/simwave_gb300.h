@@ -1,0 +1,261 @@
+/*
+ * simwave_gb300.h -- C ABI of libsimwave_gb300.so, the GB300 (sm_103a)
+ * implementation of simwave's forward time-stepping operator.
+ *
+ * Two families of entry points:
+ *
+ * 1. Host-pointer drop-ins, one per (dimension, density, precision). Each has
+ *    exactly the argument list of the reference's `forward` C function for
+ *    that variant, as marshalled by the reference's Middleware with ctypes
+ *    (simwave/kernel/backend/middleware.py:107-204): numpy arrays arrive as
+ *    pointers, Python ints as size_t, float32/float64 scalars as float/double.
+ *    `u` (num_snapshots wavefield slots) and `receivers` (end_timestep x
+ *    num_receivers) are in/out host buffers; all other arrays are read-only.
+ *    The return value is the call's wall time in seconds, as in the
+ *    reference; a negative value is an error status (see SIMWAVE_E_*), with a
+ *    message from simwave_last_error(). The library never exits the process.
+ *
+ * 2. A device-pointer entry (simwave_forward_device) that runs the same
+ *    operator on arrays already resident on the GPU, ordered on a caller's
+ *    CUDA stream, with an explicit row pitch for the fastest grid axis.
+ *
+ * Grid layout: C order of the extended grid (model + damping layer + halo),
+ * z slowest; 2D arrays are (nz, nx), 3D arrays are (nz, nx, ny).
+ * Boundary codes: 0 none, 1 null Dirichlet, 2 null Neumann, ordered
+ * (z_before, z_after, x_before, x_after[, y_before, y_after]).
+ *
+ * Difference from the reference, by design: the 3D variable-density x-axis
+ * first derivatives use the layout's row stride ny; the reference uses nx
+ * (variable_density/3d/wave.c:185-186). Results agree whenever nx == ny.
+ */
+#ifndef SIMWAVE_GB300_H
+#define SIMWAVE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error statuses (returned negated as double by the host entries) */
+#define SIMWAVE_OK 0
+#define SIMWAVE_E_ARGUMENT 1   /* invalid argument or unsupported size */
+#define SIMWAVE_E_SCHEDULE 2   /* time range / stride needs more slots */
+#define SIMWAVE_E_CUDA 3       /* CUDA runtime or launch error */
+#define SIMWAVE_E_MEMORY 4     /* device allocation failed */
+#define SIMWAVE_E_TIMEOUT 5    /* a bounded device wait gave up */
+
+/* ---- host-pointer drop-ins ------------------------------------------------
+ * replaces: forward() in
+ *   simwave/kernel/backend/c_code/forward/constant_density/2d/wave.c:23-36 */
+double simwave_forward_2d_cd_f32(
+    float *u, float *velocity, float *damp, float *wavelet,
+    size_t wavelet_size, size_t wavelet_count, float *coeff,
+    size_t *boundary_conditions, size_t *src_points_interval,
+    size_t src_points_interval_size, float *src_points_values,
+    size_t src_points_values_size, size_t *src_points_values_offset,
+    size_t *rec_points_interval, size_t rec_points_interval_size,
+    float *rec_points_values, size_t rec_points_values_size,
+    size_t *rec_points_values_offset, float *receivers, size_t num_sources,
+    size_t num_receivers, size_t nz, size_t nx, float dz, float dx,
+    size_t saving_stride, float dt, size_t begin_timestep,
+    size_t end_timestep, size_t space_order, size_t num_snapshots);
+
+/* same, built with -DDOUBLE (wave.c:17-21) */
+double simwave_forward_2d_cd_f64(
+    double *u, double *velocity, double *damp, double *wavelet,
+    size_t wavelet_size, size_t wavelet_count, double *coeff,
+    size_t *boundary_conditions, size_t *src_points_interval,
+    size_t src_points_interval_size, double *src_points_values,
+    size_t src_points_values_size, size_t *src_points_values_offset,
+    size_t *rec_points_interval, size_t rec_points_interval_size,
+    double *rec_points_values, size_t rec_points_values_size,
+    size_t *rec_points_values_offset, double *receivers, size_t num_sources,
+    size_t num_receivers, size_t nz, size_t nx, double dz, double dx,
+    size_t saving_stride, double dt, size_t begin_timestep,
+    size_t end_timestep, size_t space_order, size_t num_snapshots);
+
+/* replaces: forward() in
+ *   simwave/kernel/backend/c_code/forward/variable_density/2d/wave.c:23-36 */
+double simwave_forward_2d_vd_f32(
+    float *u, float *velocity, float *density, float *damp, float *wavelet,
+    size_t wavelet_size, size_t wavelet_count, float *coeff_order2,
+    float *coeff_order1, size_t *boundary_conditions,
+    size_t *src_points_interval, size_t src_points_interval_size,
+    float *src_points_values, size_t src_points_values_size,
+    size_t *src_points_values_offset, size_t *rec_points_interval,
+    size_t rec_points_interval_size, float *rec_points_values,
+    size_t rec_points_values_size, size_t *rec_points_values_offset,
+    float *receivers, size_t num_sources, size_t num_receivers, size_t nz,
+    size_t nx, float dz, float dx, size_t saving_stride, float dt,
+    size_t begin_timestep, size_t end_timestep, size_t space_order,
+    size_t num_snapshots);
+
+double simwave_forward_2d_vd_f64(
+    double *u, double *velocity, double *density, double *damp,
+    double *wavelet, size_t wavelet_size, size_t wavelet_count,
+    double *coeff_order2, double *coeff_order1, size_t *boundary_conditions,
+    size_t *src_points_interval, size_t src_points_interval_size,
+    double *src_points_values, size_t src_points_values_size,
+    size_t *src_points_values_offset, size_t *rec_points_interval,
+    size_t rec_points_interval_size, double *rec_points_values,
+    size_t rec_points_values_size, size_t *rec_points_values_offset,
+    double *receivers, size_t num_sources, size_t num_receivers, size_t nz,
+    size_t nx, double dz, double dx, size_t saving_stride, double dt,
+    size_t begin_timestep, size_t end_timestep, size_t space_order,
+    size_t num_snapshots);
+
+/* replaces: forward() in
+ *   simwave/kernel/backend/c_code/forward/constant_density/3d/wave.c:23-36 */
+double simwave_forward_3d_cd_f32(
+    float *u, float *velocity, float *damp, float *wavelet,
+    size_t wavelet_size, size_t wavelet_count, float *coeff,
+    size_t *boundary_conditions, size_t *src_points_interval,
+    size_t src_points_interval_size, float *src_points_values,
+    size_t src_points_values_size, size_t *src_points_values_offset,
+    size_t *rec_points_interval, size_t rec_points_interval_size,
+    float *rec_points_values, size_t rec_points_values_size,
+    size_t *rec_points_values_offset, float *receivers, size_t num_sources,
+    size_t num_receivers, size_t nz, size_t nx, size_t ny, float dz,
+    float dx, float dy, size_t saving_stride, float dt,
+    size_t begin_timestep, size_t end_timestep, size_t space_order,
+    size_t num_snapshots);
+
+double simwave_forward_3d_cd_f64(
+    double *u, double *velocity, double *damp, double *wavelet,
+    size_t wavelet_size, size_t wavelet_count, double *coeff,
+    size_t *boundary_conditions, size_t *src_points_interval,
+    size_t src_points_interval_size, double *src_points_values,
+    size_t src_points_values_size, size_t *src_points_values_offset,
+    size_t *rec_points_interval, size_t rec_points_interval_size,
+    double *rec_points_values, size_t rec_points_values_size,
+    size_t *rec_points_values_offset, double *receivers, size_t num_sources,
+    size_t num_receivers, size_t nz, size_t nx, size_t ny, double dz,
+    double dx, double dy, size_t saving_stride, double dt,
+    size_t begin_timestep, size_t end_timestep, size_t space_order,
+    size_t num_snapshots);
+
+/* replaces: forward() in
+ *   simwave/kernel/backend/c_code/forward/variable_density/3d/wave.c:23-36 */
+double simwave_forward_3d_vd_f32(
+    float *u, float *velocity, float *density, float *damp, float *wavelet,
+    size_t wavelet_size, size_t wavelet_count, float *coeff_order2,
+    float *coeff_order1, size_t *boundary_conditions,
+    size_t *src_points_interval, size_t src_points_interval_size,
+    float *src_points_values, size_t src_points_values_size,
+    size_t *src_points_values_offset, size_t *rec_points_interval,
+    size_t rec_points_interval_size, float *rec_points_values,
+    size_t rec_points_values_size, size_t *rec_points_values_offset,
+    float *receivers, size_t num_sources, size_t num_receivers, size_t nz,
+    size_t nx, size_t ny, float dz, float dx, float dy,
+    size_t saving_stride, float dt, size_t begin_timestep,
+    size_t end_timestep, size_t space_order, size_t num_snapshots);
+
+double simwave_forward_3d_vd_f64(
+    double *u, double *velocity, double *density, double *damp,
+    double *wavelet, size_t wavelet_size, size_t wavelet_count,
+    double *coeff_order2, double *coeff_order1, size_t *boundary_conditions,
+    size_t *src_points_interval, size_t src_points_interval_size,
+    double *src_points_values, size_t src_points_values_size,
+    size_t *src_points_values_offset, size_t *rec_points_interval,
+    size_t rec_points_interval_size, double *rec_points_values,
+    size_t rec_points_values_size, size_t *rec_points_values_offset,
+    double *receivers, size_t num_sources, size_t num_receivers, size_t nz,
+    size_t nx, size_t ny, double dz, double dx, double dy,
+    size_t saving_stride, double dt, size_t begin_timestep,
+    size_t end_timestep, size_t space_order, size_t num_snapshots);
+
+/* Message of the calling thread's last failed call ("" if none).
+ * No reference counterpart: the reference has no error path
+ * (C) or exits the process (cuda/wave.cu:16-24). */
+const char *simwave_last_error(void);
+
+/* ---- device-pointer entry ---------------------------------------------- */
+
+/* One forward problem on device-resident arrays. Field names follow the
+ * reference's `forward` arguments (middleware.py:160-204). All pointers
+ * marked (device) are GPU addresses; coefficients and boundary codes are read
+ * from host memory during the call.
+ *
+ * Grid arrays (u slots, velocity, density, damp) share one layout: point
+ * (i, j[, k]) of the fastest axis index f = x (2D) or y (3D) lives at
+ *   2D: i * pitch + lead + j
+ *   3D: (i * nx + j) * pitch + lead + k
+ * elements from the array base, and consecutive u slots are slot_stride
+ * elements apart. pitch >= lead + fastest extent. A dense array has
+ * pitch = fastest extent and lead = 0. */
+typedef struct simwave_problem {
+    int dim;                  /* 2 or 3 */
+    int variable_density;     /* 0 constant, 1 variable */
+    int precision;            /* 4 (float32) or 8 (float64) */
+    int space_order;          /* even, 2..20 */
+    size_t nz, nx, ny;        /* extended shape; ny = 1 in 2D */
+    size_t pitch, lead, slot_stride;
+    double dz, dx, dy, dt;
+    void *u;                  /* (device) num_snapshots slots, in/out */
+    size_t num_snapshots;
+    const void *velocity;     /* (device) */
+    const void *density;      /* (device) NULL for constant density */
+    const void *damp;         /* (device) */
+    const void *wavelet;      /* (device) wavelet_size * wavelet_count */
+    size_t wavelet_size, wavelet_count;
+    const void *coeff_order2; /* (host) space_order/2 + 1 values */
+    const void *coeff_order1; /* (host) idem, variable density only */
+    const size_t *boundary_conditions;      /* (host) 2*dim codes */
+    const size_t *src_points_interval;      /* (device) 2*dim per source */
+    const void *src_points_values;          /* (device) */
+    const size_t *src_points_values_offset; /* (device) num_sources + 1 */
+    size_t src_points_values_size;
+    size_t num_sources;
+    const size_t *rec_points_interval;      /* (device) */
+    const void *rec_points_values;          /* (device) */
+    const size_t *rec_points_values_offset; /* (device) */
+    size_t rec_points_values_size;
+    size_t num_receivers;
+    void *receivers;          /* (device) end_timestep * num_receivers, out */
+    size_t saving_stride, begin_timestep, end_timestep;
+    unsigned flags;           /* SIMWAVE_FLAG_* */
+} simwave_problem;
+
+/* flags */
+#define SIMWAVE_FLAG_TIME_KERNELS 1u  /* time the stencil launches (events) */
+#define SIMWAVE_FLAG_WINDOWS_CHECKED 2u /* caller validated the KWS windows
+                                          (intervals inside the grid, offsets
+                                          consistent); skips the device->host
+                                          copy the library otherwise makes to
+                                          check them */
+
+/* Preferred layout of the fastest axis for a grid of `fastest_extent`
+ * points at `space_order` and `precision` bytes: writes the row pitch and
+ * leading offset (elements) that align each row's first interior point to
+ * 128 bytes. Returns SIMWAVE_OK or SIMWAVE_E_ARGUMENT.
+ * No reference counterpart (the reference uses dense arrays). */
+int simwave_layout(size_t fastest_extent, int space_order, int precision,
+                   size_t *pitch, size_t *lead);
+
+/* Run the forward loop on `stream` (a cudaStream_t, NULL = default stream).
+ * Returns SIMWAVE_OK or an error status; the work is stream-ordered and the
+ * call returns before it completes unless SIMWAVE_FLAG_TIME_KERNELS is set
+ * (then it synchronises the stream to read the timers).
+ * No reference counterpart: the reference allocates and copies per call. */
+int simwave_forward_device(const simwave_problem *problem, void *stream);
+
+/* Statistics of the calling thread's last successful forward call. */
+typedef struct simwave_stats {
+    double seconds;           /* wall time of the call */
+    double stencil_ms;        /* summed stencil kernel time (if timed) */
+    double updates;           /* interior point updates performed */
+    size_t stencil_launches;  /* stencil kernel launches */
+    size_t kernel_launches;   /* all kernel launches of this library */
+    size_t h2d_bytes, d2h_bytes;
+    int stencil_variant;      /* 0 generic, 1 tiled */
+} simwave_stats;
+
+/* No reference counterpart (the reference returns only its wall time). */
+int simwave_last_stats(simwave_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMWAVE_GB300_H */

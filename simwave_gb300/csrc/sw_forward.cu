@@ -1,0 +1,838 @@
+// sw_forward.cu -- host driver and C ABI of libsimwave_gb300.so.
+//
+// Owns: argument validation, the time-level slot schedule, device buffers of
+// the host-pointer entries, kernel launch sequence per time step, timing and
+// error reporting. Kernels live in sw_kernels.cuh (generic) and
+// sw_stencil_tiled.cu (tiled fast path).
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "simwave_gb300.h"
+#include "sw_kernels.cuh"
+#include "sw_tiled.h"
+
+namespace sw {
+
+// ---------------------------------------------------------------------------
+// errors
+
+struct Failure {
+    int code;
+    std::string message;
+};
+
+static thread_local std::string g_last_error;
+static thread_local simwave_stats g_last_stats;
+
+[[noreturn]] static void fail(int code, const std::string& msg) {
+    throw Failure{code, msg};
+}
+
+#define SW_CUDA(expr)                                                       \
+    do {                                                                    \
+        cudaError_t e_ = (expr);                                            \
+        if (e_ != cudaSuccess)                                              \
+            ::sw::fail(e_ == cudaErrorMemoryAllocation ? SIMWAVE_E_MEMORY   \
+                                                       : SIMWAVE_E_CUDA,    \
+                       std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define SW_LAUNCHED(name)                                                   \
+    do {                                                                    \
+        cudaError_t e_ = cudaGetLastError();                                \
+        if (e_ != cudaSuccess)                                              \
+            ::sw::fail(SIMWAVE_E_CUDA,                                      \
+                       std::string("launch ") + name + ": " +               \
+                           cudaGetErrorString(e_));                         \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// slot schedule
+//
+// The reference keeps every time level in a slot of `u` and moves three slot
+// indices (prev, cur, next) per step (constant_density/2d/wave.c:110-122,
+// 466-514): stride 0 rotates through slots 0..2, stride 1 writes level n+1
+// into slot n+1, stride s > 1 advances one slot every s steps and, for even
+// s, exchanges the contents of two slots. The schedule below replays that
+// bookkeeping on the host. The exchange is realised as a relabelling of
+// physical slots (perm), so no data moves; final contents of logical slot j
+// are in physical slot perm[j].
+
+struct StepSlots {
+    int prev, cur, next;  // physical slots
+};
+
+struct Schedule {
+    std::vector<StepSlots> steps;
+    std::vector<int> perm;     // logical -> physical at the end
+    std::vector<char> written; // physical slot written at least once
+    std::vector<char> touched; // logical slot read or written
+};
+
+static Schedule make_schedule(size_t begin, size_t end, size_t stride,
+                              size_t nslots) {
+    Schedule S;
+    S.perm.resize(nslots);
+    for (size_t i = 0; i < nslots; i++) S.perm[i] = (int)i;
+    S.written.assign(nslots, 0);
+    S.touched.assign(nslots, 0);
+    if (begin < 1) fail(SIMWAVE_E_ARGUMENT, "begin_timestep must be >= 1");
+    size_t prev = 0, cur = 1, next = 2;
+    for (size_t n = begin; n <= end; n++) {
+        if (stride == 0) {
+            prev = (n - 1) % 3;
+            cur = n % 3;
+            next = (n + 1) % 3;
+        } else if (stride == 1) {
+            prev = n - 1;
+            cur = n;
+            next = n + 1;
+        }
+        if (prev >= nslots || cur >= nslots || next >= nslots)
+            fail(SIMWAVE_E_SCHEDULE,
+                 "time step " + std::to_string(n) + " needs wavefield slot " +
+                     std::to_string(std::max(prev, std::max(cur, next))) +
+                     " but num_snapshots is " + std::to_string(nslots));
+        S.steps.push_back({S.perm[prev], S.perm[cur], S.perm[next]});
+        S.written[S.perm[next]] = 1;
+        S.touched[prev] = S.touched[cur] = S.touched[next] = 1;
+        if (stride > 1) {
+            if (n % stride == 1) {
+                prev = cur;
+                cur += 1;
+                next += 1;
+                if (stride % 2 == 0 && n < end) {
+                    std::swap(cur, next);
+                    if (cur >= nslots || next >= nslots)
+                        fail(SIMWAVE_E_SCHEDULE,
+                             "even-stride exchange needs slot " +
+                                 std::to_string(std::max(cur, next)) +
+                                 " but num_snapshots is " +
+                                 std::to_string(nslots));
+                    std::swap(S.perm[cur], S.perm[next]);
+                    S.touched[cur] = S.touched[next] = 1;
+                }
+            } else {
+                prev = cur;
+                cur = next;
+                next = prev;
+            }
+        }
+    }
+    return S;
+}
+
+// ---------------------------------------------------------------------------
+// layout
+
+static void choose_layout(size_t nfast, int r, int precision, size_t* pitch,
+                          size_t* lead) {
+    const size_t align = 128 / (size_t)precision;  // elements per 128 B
+    *lead = (align - (size_t)r % align) % align;
+    *pitch = (*lead + nfast + align - 1) / align * align;
+}
+
+// ---------------------------------------------------------------------------
+// device buffers owned by the host-pointer entries (grow-only, per device)
+
+struct Buffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    void* ensure(size_t n) {
+        if (n <= bytes) return ptr;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        if (n == 0) return nullptr;
+        SW_CUDA(cudaMalloc(&ptr, n));
+        bytes = n;
+        return ptr;
+    }
+};
+
+struct Arena {
+    Buffer u, vel, den, damp, wavelet, rec;
+    Buffer src_iv, src_val, src_off, rec_iv, rec_val, rec_off;
+    Buffer scratch;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> events;
+};
+
+static std::mutex g_mutex;  // serialises the host-pointer entries
+static std::map<int, Arena> g_arenas;
+
+static Arena& arena_for_current_device() {
+    int dev = 0;
+    SW_CUDA(cudaGetDevice(&dev));
+    Arena& a = g_arenas[dev];
+    if (!a.stream) SW_CUDA(cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking));
+    return a;
+}
+
+static std::mutex g_event_mutex;
+static std::map<int, std::vector<cudaEvent_t>> g_event_pool;
+
+// ---------------------------------------------------------------------------
+// one forward run on device-resident data
+
+template <typename T>
+struct Run {
+    Layout L;
+    bool vd;
+    T* u;
+    size_t nslots;
+    const T* vel;
+    const T* den;
+    const T* damp;
+    const T* wavelet;
+    size_t wavelet_count;
+    Weights<T> W;
+    int bc[6];
+    Windows<T> src, rec;
+    T* receivers;
+    size_t begin, end, stride;
+    T dt;
+    unsigned flags;
+};
+
+template <typename T>
+static Weights<T> make_weights(const T* c2, const T* c1, int r, double dz,
+                               double dx, double dy) {
+    Weights<T> W;
+    std::memset(&W, 0, sizeof(W));
+    const double h[3] = {dz, dx, dy};
+    for (int a = 0; a < 3; a++) {
+        const double h2 = h[a] * h[a];
+        for (int k = 0; k <= r; k++) W.c2[a][k] = (T)((double)c2[k] / h2);
+        W.s1[a] = (T)(1.0 / (4.0 * h2));
+    }
+    for (int k = 0; k <= r; k++) W.c1[k] = c1 ? c1[k] : T(0);
+    return W;
+}
+
+template <typename T, int DIM, bool VD>
+static void launch_stencil(const Run<T>& R, T* un, const T* uc, const T* up,
+                           cudaStream_t st, int* variant) {
+    const Layout& L = R.L;
+    const T dt2 = R.dt * R.dt;
+    if (tiled_supported<T, DIM, VD>(L)) {
+        launch_tiled<T, DIM, VD>(un, uc, up, R.vel, R.den, R.damp, L, R.W,
+                                 R.dt, dt2, st);
+        *variant = 1;
+        SW_LAUNCHED("stencil_tiled");
+        return;
+    }
+    const int r = L.r;
+    dim3 block(32, 8, 1);
+    dim3 grid((unsigned)((L.nfast() - 2 * r + 31) / 32),
+              (unsigned)((L.nmid() - 2 * r + 7) / 8),
+              DIM == 3 ? (unsigned)(L.nslow() - 2 * r) : 1u);
+    stencil_generic<T, DIM, VD><<<grid, block, 0, st>>>(
+        un, uc, up, R.vel, R.den, R.damp, L, R.W, R.dt, dt2);
+    *variant = 0;
+    SW_LAUNCHED("stencil_generic");
+}
+
+template <typename T, int DIM, bool VD>
+static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
+                      simwave_stats& stats, std::vector<cudaEvent_t>* ev) {
+    const Layout& L = R.L;
+    const T dt2 = R.dt * R.dt;
+    // boundary phases in the reference's order: y, x, z (3D); x, z (2D)
+    int phases[3], nphase = 0;
+    if (DIM == 3) { phases[0] = 2; phases[1] = 1; phases[2] = 0; nphase = 3; }
+    else { phases[0] = 1; phases[1] = 0; nphase = 2; }
+    for (size_t i = 0; i < S.steps.size(); i++) {
+        const size_t n = R.begin + i;
+        T* un = R.u + (size_t)S.steps[i].next * L.slot;
+        const T* uc = R.u + (size_t)S.steps[i].cur * L.slot;
+        const T* up = R.u + (size_t)S.steps[i].prev * L.slot;
+        if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i], st));
+        launch_stencil<T, DIM, VD>(R, un, uc, up, st, &stats.stencil_variant);
+        if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i + 1], st));
+        stats.stencil_launches++;
+        stats.kernel_launches++;
+        if (R.src.count) {
+            inject_sources<T, DIM><<<(unsigned)R.src.count, 128, 0, st>>>(
+                un, R.vel, R.damp, L, R.src, R.wavelet, R.wavelet_count, n,
+                R.dt, dt2);
+            SW_LAUNCHED("inject_sources");
+            stats.kernel_launches++;
+        }
+        for (int ph = 0; ph < nphase; ph++) {
+            const int a = phases[ph];
+            const int b0 = R.bc[2 * a], b1 = R.bc[2 * a + 1];
+            if (b0 == 0 && b1 == 0) continue;
+            const int a1 = a == 0 ? 1 : 0;
+            const int a2 = DIM == 3 ? (a == 2 ? 1 : 2) : -1;
+            const long long lines = (L.extent(a1) - 2 * L.r) *
+                                    (a2 >= 0 ? L.extent(a2) - 2 * L.r : 1);
+            boundary_phase<T><<<(unsigned)((lines + 255) / 256), 256, 0, st>>>(
+                un, L, a, b0, b1);
+            SW_LAUNCHED("boundary_phase");
+            stats.kernel_launches++;
+        }
+        if (R.rec.count) {
+            const size_t threads = R.rec.count * 32;
+            record_receivers<T, DIM><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                R.receivers + (n - 1) * R.rec.count, uc, L, R.rec);
+            SW_LAUNCHED("record_receivers");
+            stats.kernel_launches++;
+        }
+    }
+}
+
+template <typename T>
+static void dispatch_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
+                           simwave_stats& stats, std::vector<cudaEvent_t>* ev) {
+    if (R.L.dim == 2 && !R.vd) run_steps<T, 2, false>(R, S, st, stats, ev);
+    else if (R.L.dim == 2) run_steps<T, 2, true>(R, S, st, stats, ev);
+    else if (!R.vd) run_steps<T, 3, false>(R, S, st, stats, ev);
+    else run_steps<T, 3, true>(R, S, st, stats, ev);
+}
+
+// ---------------------------------------------------------------------------
+// validation of sizes and KWS windows (host copies)
+
+static void check_grid(int dim, int order, size_t nz, size_t nx, size_t ny) {
+    if (dim != 2 && dim != 3) fail(SIMWAVE_E_ARGUMENT, "dim must be 2 or 3");
+    if (order < 2 || order > 20 || order % 2)
+        fail(SIMWAVE_E_ARGUMENT, "space_order must be even in 2..20, got " +
+                                     std::to_string(order));
+    const size_t r = order / 2;
+    const size_t ext[3] = {nz, nx, dim == 3 ? ny : 2 * r + 1};
+    for (int a = 0; a < 3; a++)
+        if (ext[a] < 2 * r + 1)
+            fail(SIMWAVE_E_ARGUMENT,
+                 "every grid extent must be >= space_order + 1");
+    if ((double)nz * nx * (dim == 3 ? ny : 1) > 9.0e15)
+        fail(SIMWAVE_E_ARGUMENT, "grid too large");
+}
+
+static void check_windows(const char* what, int dim, const size_t* iv,
+                          size_t iv_size, const size_t* off,
+                          size_t values_size, size_t count,
+                          const size_t ext[3]) {
+    if (count == 0) return;
+    if (!iv || !off) fail(SIMWAVE_E_ARGUMENT, std::string(what) + " arrays missing");
+    if (iv_size < count * 2 * dim)
+        fail(SIMWAVE_E_ARGUMENT, std::string(what) + "_points_interval too short");
+    for (size_t s = 0; s < count; s++) {
+        size_t len = 0;
+        for (int a = 0; a < dim; a++) {
+            const size_t b = iv[s * 2 * dim + 2 * a], e = iv[s * 2 * dim + 2 * a + 1];
+            if (b > e || e >= ext[a])
+                fail(SIMWAVE_E_ARGUMENT, std::string(what) + " " +
+                                             std::to_string(s) +
+                                             ": window outside the grid");
+            len += e - b + 1;
+        }
+        if (off[s] > values_size || len > values_size - off[s])
+            fail(SIMWAVE_E_ARGUMENT, std::string(what) + " " +
+                                         std::to_string(s) +
+                                         ": values offset out of range");
+    }
+}
+
+static void check_time(size_t begin, size_t end, size_t wavelet_size,
+                       size_t wavelet_count, size_t nsrc) {
+    if (begin < 1) fail(SIMWAVE_E_ARGUMENT, "begin_timestep must be >= 1");
+    if (end < begin) return;
+    if (nsrc == 0) return;
+    const size_t need = wavelet_count > 1 ? end * nsrc : end;
+    if (wavelet_size * std::max<size_t>(wavelet_count, 1) < need)
+        fail(SIMWAVE_E_ARGUMENT, "wavelet shorter than end_timestep");
+}
+
+// ---------------------------------------------------------------------------
+// host-pointer entry
+
+template <typename T>
+struct HostArgs {
+    int dim;
+    bool vd;
+    T* u;
+    const T* vel;
+    const T* den;
+    const T* damp;
+    const T* wavelet;
+    size_t wavelet_size, wavelet_count;
+    const T* c2;
+    const T* c1;
+    const size_t* bc;
+    const size_t* src_iv;
+    size_t src_iv_size;
+    const T* src_val;
+    size_t src_val_size;
+    const size_t* src_off;
+    const size_t* rec_iv;
+    size_t rec_iv_size;
+    const T* rec_val;
+    size_t rec_val_size;
+    const size_t* rec_off;
+    T* receivers;
+    size_t nsrc, nrec, nz, nx, ny;
+    T dz, dx, dy;
+    size_t stride;
+    T dt;
+    size_t begin, end, order, nslots;
+};
+
+template <typename T>
+static void copy_grid_h2d(T* dst, const T* src, const Layout& L,
+                          cudaStream_t st, size_t* bytes) {
+    const size_t nf = (size_t)L.nfast();
+    const size_t rows = (size_t)(L.dim == 3 ? L.nz * L.nx : L.nz);
+    SW_CUDA(cudaMemcpy2DAsync(dst + L.lead, L.pitch * sizeof(T), src,
+                              nf * sizeof(T), nf * sizeof(T), rows,
+                              cudaMemcpyHostToDevice, st));
+    *bytes += rows * nf * sizeof(T);
+}
+
+template <typename T>
+static void copy_grid_d2h(T* dst, const T* src, const Layout& L,
+                          cudaStream_t st, size_t* bytes) {
+    const size_t nf = (size_t)L.nfast();
+    const size_t rows = (size_t)(L.dim == 3 ? L.nz * L.nx : L.nz);
+    SW_CUDA(cudaMemcpy2DAsync(dst, nf * sizeof(T), src + L.lead,
+                              L.pitch * sizeof(T), nf * sizeof(T), rows,
+                              cudaMemcpyDeviceToHost, st));
+    *bytes += rows * nf * sizeof(T);
+}
+
+template <typename T>
+static void* upload(Buffer& b, const void* src, size_t bytes, cudaStream_t st,
+                    size_t* counted) {
+    void* p = b.ensure(std::max<size_t>(bytes, 16));
+    if (bytes) SW_CUDA(cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, st));
+    *counted += bytes;
+    return p;
+}
+
+template <typename T>
+static double host_forward(const HostArgs<T>& A) {
+    const auto t0 = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lock(g_mutex);
+    simwave_stats stats;
+    std::memset(&stats, 0, sizeof(stats));
+
+    check_grid(A.dim, (int)A.order, A.nz, A.nx, A.ny);
+    const size_t ext[3] = {A.nz, A.nx, A.dim == 3 ? A.ny : 1};
+    if (!A.u || !A.vel || !A.damp || (A.vd && (!A.den || !A.c1)) || !A.c2 ||
+        !A.bc || (A.nrec && !A.receivers) || (A.nsrc && !A.wavelet))
+        fail(SIMWAVE_E_ARGUMENT, "null array argument");
+    for (int e = 0; e < 2 * A.dim; e++)
+        if (A.bc[e] > 2) fail(SIMWAVE_E_ARGUMENT, "boundary code must be 0, 1 or 2");
+    check_windows("src", A.dim, A.src_iv, A.src_iv_size, A.src_off,
+                  A.src_val_size, A.nsrc, ext);
+    check_windows("rec", A.dim, A.rec_iv, A.rec_iv_size, A.rec_off,
+                  A.rec_val_size, A.nrec, ext);
+    check_time(A.begin, A.end, A.wavelet_size, A.wavelet_count, A.nsrc);
+    Schedule S = make_schedule(A.begin, A.end, A.stride, A.nslots);
+
+    Layout L;
+    L.dim = A.dim;
+    L.r = (int)(A.order / 2);
+    L.nz = (long long)A.nz;
+    L.nx = (long long)A.nx;
+    L.ny = A.dim == 3 ? (long long)A.ny : 1;
+    size_t pitch, lead;
+    choose_layout((size_t)L.nfast(), L.r, (int)sizeof(T), &pitch, &lead);
+    L.pitch = (long long)pitch;
+    L.lead = (long long)lead;
+    L.plane = A.dim == 3 ? L.nx * L.pitch : L.pitch;
+    L.slot = A.dim == 3 ? L.nz * L.plane : L.nz * L.pitch;
+
+    Arena& ar = arena_for_current_device();
+    cudaStream_t st = ar.stream;
+    const size_t slot_bytes = (size_t)L.slot * sizeof(T);
+    T* du = (T*)ar.u.ensure(slot_bytes * A.nslots);
+    T* dvel = (T*)ar.vel.ensure(slot_bytes);
+    T* dden = A.vd ? (T*)ar.den.ensure(slot_bytes) : nullptr;
+    T* ddamp = (T*)ar.damp.ensure(slot_bytes);
+    const size_t rec_rows = A.end >= A.begin ? A.end - A.begin + 1 : 0;
+    T* drec = (T*)ar.rec.ensure(std::max<size_t>(A.end * A.nrec * sizeof(T), 16));
+
+    size_t h2d = 0, d2h = 0;
+    for (size_t j = 0; j < A.nslots; j++)
+        if (S.touched[j]) copy_grid_h2d(du + j * L.slot, A.u + j * L.nz * L.nx * L.ny, L, st, &h2d);
+    copy_grid_h2d(dvel, A.vel, L, st, &h2d);
+    if (A.vd) copy_grid_h2d(dden, A.den, L, st, &h2d);
+    copy_grid_h2d(ddamp, A.damp, L, st, &h2d);
+    const size_t wlen = A.wavelet_size * std::max<size_t>(A.wavelet_count, 1);
+    T* dw = (T*)upload<T>(ar.wavelet, A.wavelet, A.nsrc ? wlen * sizeof(T) : 0, st, &h2d);
+    size_t* dsiv = (size_t*)upload<T>(ar.src_iv, A.src_iv, A.nsrc * 2 * A.dim * sizeof(size_t), st, &h2d);
+    T* dsval = (T*)upload<T>(ar.src_val, A.src_val, A.nsrc ? A.src_val_size * sizeof(T) : 0, st, &h2d);
+    size_t* dsoff = (size_t*)upload<T>(ar.src_off, A.src_off, A.nsrc ? A.nsrc * sizeof(size_t) : 0, st, &h2d);
+    size_t* driv = (size_t*)upload<T>(ar.rec_iv, A.rec_iv, A.nrec * 2 * A.dim * sizeof(size_t), st, &h2d);
+    T* drval = (T*)upload<T>(ar.rec_val, A.rec_val, A.nrec ? A.rec_val_size * sizeof(T) : 0, st, &h2d);
+    size_t* droff = (size_t*)upload<T>(ar.rec_off, A.rec_off, A.nrec ? A.nrec * sizeof(size_t) : 0, st, &h2d);
+
+    Run<T> R;
+    R.L = L;
+    R.vd = A.vd;
+    R.u = du;
+    R.nslots = A.nslots;
+    R.vel = dvel;
+    R.den = dden;
+    R.damp = ddamp;
+    R.wavelet = dw;
+    R.wavelet_count = A.wavelet_count;
+    R.W = make_weights<T>(A.c2, A.vd ? A.c1 : nullptr, L.r, (double)A.dz,
+                          (double)A.dx, A.dim == 3 ? (double)A.dy : 1.0);
+    for (int e = 0; e < 6; e++) R.bc[e] = e < 2 * A.dim ? (int)A.bc[e] : 0;
+    R.src = Windows<T>{dsiv, dsval, dsoff, A.nsrc};
+    R.rec = Windows<T>{driv, drval, droff, A.nrec};
+    R.receivers = drec;
+    R.begin = A.begin;
+    R.end = A.end;
+    R.stride = A.stride;
+    R.dt = A.dt;
+    R.flags = 0;
+    dispatch_steps<T>(R, S, st, stats, nullptr);
+
+    // results: every slot that may have changed, and the receiver rows written
+    for (size_t j = 0; j < A.nslots; j++) {
+        const int phys = S.perm[j];
+        if (S.written[phys] || phys != (int)j)
+            copy_grid_d2h(A.u + j * L.nz * L.nx * L.ny, du + (size_t)phys * L.slot, L, st, &d2h);
+    }
+    if (rec_rows && A.nrec) {
+        const size_t off = (A.begin - 1) * A.nrec;
+        SW_CUDA(cudaMemcpyAsync(A.receivers + off, drec + off,
+                                rec_rows * A.nrec * sizeof(T),
+                                cudaMemcpyDeviceToHost, st));
+        d2h += rec_rows * A.nrec * sizeof(T);
+    }
+    SW_CUDA(cudaStreamSynchronize(st));
+    const double secs =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats.seconds = secs;
+    stats.updates = (double)L.interior_points() * (double)S.steps.size();
+    stats.h2d_bytes = h2d;
+    stats.d2h_bytes = d2h;
+    g_last_stats = stats;
+    return secs;
+}
+
+template <typename T>
+static double host_entry(const HostArgs<T>& A) {
+    try {
+        g_last_error.clear();
+        return host_forward<T>(A);
+    } catch (const Failure& f) {
+        g_last_error = f.message;
+        return -(double)f.code;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return -(double)SIMWAVE_E_ARGUMENT;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// device-pointer entry
+
+template <typename T>
+static int device_forward(const simwave_problem* P, cudaStream_t st) {
+    const auto t0 = std::chrono::steady_clock::now();
+    simwave_stats stats;
+    std::memset(&stats, 0, sizeof(stats));
+    if (!P) fail(SIMWAVE_E_ARGUMENT, "null problem");
+    check_grid(P->dim, P->space_order, P->nz, P->nx, P->ny);
+    const bool vd = P->variable_density != 0;
+    const size_t ext[3] = {P->nz, P->nx, P->dim == 3 ? P->ny : 1};
+    if (!P->u || !P->velocity || !P->damp || (vd && (!P->density || !P->coeff_order1)) ||
+        !P->coeff_order2 || !P->boundary_conditions ||
+        (P->num_receivers && !P->receivers) || (P->num_sources && !P->wavelet))
+        fail(SIMWAVE_E_ARGUMENT, "null array argument");
+    for (int e = 0; e < 2 * P->dim; e++)
+        if (P->boundary_conditions[e] > 2)
+            fail(SIMWAVE_E_ARGUMENT, "boundary code must be 0, 1 or 2");
+    const size_t nfast = P->dim == 3 ? P->ny : P->nx;
+    if (P->pitch < P->lead + nfast) fail(SIMWAVE_E_ARGUMENT, "pitch < lead + fastest extent");
+    const size_t grid_elems = P->dim == 3 ? P->nz * P->nx * P->pitch : P->nz * P->pitch;
+    if (P->num_snapshots > 1 && P->slot_stride < grid_elems)
+        fail(SIMWAVE_E_ARGUMENT, "slot_stride smaller than one grid");
+    check_time(P->begin_timestep, P->end_timestep, P->wavelet_size,
+               P->wavelet_count, P->num_sources);
+    if (!(P->flags & SIMWAVE_FLAG_WINDOWS_CHECKED)) {
+        // copy the windows to the host and check them
+        for (int which = 0; which < 2; which++) {
+            const size_t count = which ? P->num_receivers : P->num_sources;
+            if (!count) continue;
+            const size_t* div = which ? P->rec_points_interval : P->src_points_interval;
+            const size_t* doff = which ? P->rec_points_values_offset : P->src_points_values_offset;
+            std::vector<size_t> iv(count * 2 * P->dim), off(count);
+            SW_CUDA(cudaMemcpyAsync(iv.data(), div, iv.size() * sizeof(size_t),
+                                    cudaMemcpyDeviceToHost, st));
+            SW_CUDA(cudaMemcpyAsync(off.data(), doff, off.size() * sizeof(size_t),
+                                    cudaMemcpyDeviceToHost, st));
+            SW_CUDA(cudaStreamSynchronize(st));
+            check_windows(which ? "rec" : "src", P->dim, iv.data(), iv.size(),
+                          off.data(),
+                          which ? P->rec_points_values_size : P->src_points_values_size,
+                          count, ext);
+        }
+    }
+    Schedule S = make_schedule(P->begin_timestep, P->end_timestep,
+                               P->saving_stride, P->num_snapshots);
+    Layout L;
+    L.dim = P->dim;
+    L.r = P->space_order / 2;
+    L.nz = (long long)P->nz;
+    L.nx = (long long)P->nx;
+    L.ny = P->dim == 3 ? (long long)P->ny : 1;
+    L.pitch = (long long)P->pitch;
+    L.lead = (long long)P->lead;
+    L.plane = P->dim == 3 ? L.nx * L.pitch : L.pitch;
+    L.slot = (long long)P->slot_stride;
+
+    Run<T> R;
+    R.L = L;
+    R.vd = vd;
+    R.u = (T*)P->u;
+    R.nslots = P->num_snapshots;
+    R.vel = (const T*)P->velocity;
+    R.den = (const T*)P->density;
+    R.damp = (const T*)P->damp;
+    R.wavelet = (const T*)P->wavelet;
+    R.wavelet_count = P->wavelet_count;
+    R.W = make_weights<T>((const T*)P->coeff_order2,
+                          vd ? (const T*)P->coeff_order1 : nullptr, L.r, P->dz,
+                          P->dx, P->dim == 3 ? P->dy : 1.0);
+    for (int e = 0; e < 6; e++)
+        R.bc[e] = e < 2 * P->dim ? (int)P->boundary_conditions[e] : 0;
+    R.src = Windows<T>{P->src_points_interval, (const T*)P->src_points_values,
+                       P->src_points_values_offset, P->num_sources};
+    R.rec = Windows<T>{P->rec_points_interval, (const T*)P->rec_points_values,
+                       P->rec_points_values_offset, P->num_receivers};
+    R.receivers = (T*)P->receivers;
+    R.begin = P->begin_timestep;
+    R.end = P->end_timestep;
+    R.stride = P->saving_stride;
+    R.dt = (T)P->dt;
+    R.flags = P->flags;
+
+    std::vector<cudaEvent_t>* ev = nullptr;
+    std::vector<cudaEvent_t> events;
+    if (P->flags & SIMWAVE_FLAG_TIME_KERNELS) {
+        int dev = 0;
+        SW_CUDA(cudaGetDevice(&dev));
+        std::lock_guard<std::mutex> lock(g_event_mutex);
+        auto& pool = g_event_pool[dev];
+        while (pool.size() < 2 * S.steps.size()) {
+            cudaEvent_t e;
+            SW_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        events.assign(pool.begin(), pool.begin() + 2 * S.steps.size());
+        ev = &events;
+    }
+    dispatch_steps<T>(R, S, st, stats, ev);
+
+    // restore the logical slot order where the even-stride exchanges moved it
+    bool moved = false;
+    for (size_t j = 0; j < P->num_snapshots; j++) moved |= S.perm[j] != (int)j;
+    if (moved) {
+        int dev = 0;
+        SW_CUDA(cudaGetDevice(&dev));
+        Buffer* scratch;
+        {
+            std::lock_guard<std::mutex> lock(g_mutex);
+            scratch = &g_arenas[dev].scratch;
+        }
+        const size_t bytes = grid_elems * sizeof(T);
+        T* tmp = (T*)scratch->ensure(bytes);
+        std::vector<char> done(P->num_snapshots, 0);
+        T* base = (T*)P->u;
+        for (size_t j = 0; j < P->num_snapshots; j++) {
+            if (done[j] || S.perm[j] == (int)j) continue;
+            // cycle j <- perm[j] <- perm[perm[j]] ...
+            SW_CUDA(cudaMemcpyAsync(tmp, base + j * L.slot, bytes, cudaMemcpyDeviceToDevice, st));
+            size_t cur = j;
+            while (true) {
+                const size_t src = (size_t)S.perm[cur];
+                done[cur] = 1;
+                if (src == j) {
+                    SW_CUDA(cudaMemcpyAsync(base + cur * L.slot, tmp, bytes, cudaMemcpyDeviceToDevice, st));
+                    break;
+                }
+                SW_CUDA(cudaMemcpyAsync(base + cur * L.slot, base + src * L.slot, bytes,
+                                        cudaMemcpyDeviceToDevice, st));
+                cur = src;
+            }
+        }
+    }
+    if (ev) {
+        SW_CUDA(cudaStreamSynchronize(st));
+        double ms = 0;
+        for (size_t i = 0; i < S.steps.size(); i++) {
+            float t = 0;
+            SW_CUDA(cudaEventElapsedTime(&t, events[2 * i], events[2 * i + 1]));
+            ms += t;
+        }
+        stats.stencil_ms = ms;
+    }
+    stats.seconds =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats.updates = (double)L.interior_points() * (double)S.steps.size();
+    g_last_stats = stats;
+    return SIMWAVE_OK;
+}
+
+}  // namespace sw
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+using sw::HostArgs;
+
+#define SW_HOST_ARGS_COMMON(T)                                                \
+    A.wavelet = wavelet; A.wavelet_size = wavelet_size;                       \
+    A.wavelet_count = wavelet_count; A.bc = boundary_conditions;              \
+    A.src_iv = src_points_interval; A.src_iv_size = src_points_interval_size; \
+    A.src_val = src_points_values; A.src_val_size = src_points_values_size;   \
+    A.src_off = src_points_values_offset; A.rec_iv = rec_points_interval;     \
+    A.rec_iv_size = rec_points_interval_size; A.rec_val = rec_points_values;  \
+    A.rec_val_size = rec_points_values_size;                                  \
+    A.rec_off = rec_points_values_offset; A.receivers = receivers;            \
+    A.nsrc = num_sources; A.nrec = num_receivers; A.stride = saving_stride;   \
+    A.dt = dt; A.begin = begin_timestep; A.end = end_timestep;                \
+    A.order = space_order; A.nslots = num_snapshots; A.u = u;                 \
+    A.vel = velocity; A.damp = damp;
+
+#define SW_DEFINE_2D_CD(SFX, T)                                               \
+    extern "C" double simwave_forward_2d_cd_##SFX(                            \
+        T* u, T* velocity, T* damp, T* wavelet, size_t wavelet_size,          \
+        size_t wavelet_count, T* coeff, size_t* boundary_conditions,          \
+        size_t* src_points_interval, size_t src_points_interval_size,         \
+        T* src_points_values, size_t src_points_values_size,                  \
+        size_t* src_points_values_offset, size_t* rec_points_interval,        \
+        size_t rec_points_interval_size, T* rec_points_values,                \
+        size_t rec_points_values_size, size_t* rec_points_values_offset,      \
+        T* receivers, size_t num_sources, size_t num_receivers, size_t nz,    \
+        size_t nx, T dz, T dx, size_t saving_stride, T dt,                    \
+        size_t begin_timestep, size_t end_timestep, size_t space_order,       \
+        size_t num_snapshots) {                                               \
+        HostArgs<T> A{};                                                      \
+        SW_HOST_ARGS_COMMON(T)                                                \
+        A.dim = 2; A.vd = false; A.den = nullptr; A.c2 = coeff;               \
+        A.c1 = nullptr; A.nz = nz; A.nx = nx; A.ny = 1; A.dz = dz;            \
+        A.dx = dx; A.dy = 1;                                                  \
+        return sw::host_entry<T>(A);                                          \
+    }
+
+#define SW_DEFINE_2D_VD(SFX, T)                                               \
+    extern "C" double simwave_forward_2d_vd_##SFX(                            \
+        T* u, T* velocity, T* density, T* damp, T* wavelet,                   \
+        size_t wavelet_size, size_t wavelet_count, T* coeff_order2,           \
+        T* coeff_order1, size_t* boundary_conditions,                         \
+        size_t* src_points_interval, size_t src_points_interval_size,         \
+        T* src_points_values, size_t src_points_values_size,                  \
+        size_t* src_points_values_offset, size_t* rec_points_interval,        \
+        size_t rec_points_interval_size, T* rec_points_values,                \
+        size_t rec_points_values_size, size_t* rec_points_values_offset,      \
+        T* receivers, size_t num_sources, size_t num_receivers, size_t nz,    \
+        size_t nx, T dz, T dx, size_t saving_stride, T dt,                    \
+        size_t begin_timestep, size_t end_timestep, size_t space_order,       \
+        size_t num_snapshots) {                                               \
+        HostArgs<T> A{};                                                      \
+        SW_HOST_ARGS_COMMON(T)                                                \
+        A.dim = 2; A.vd = true; A.den = density; A.c2 = coeff_order2;         \
+        A.c1 = coeff_order1; A.nz = nz; A.nx = nx; A.ny = 1; A.dz = dz;       \
+        A.dx = dx; A.dy = 1;                                                  \
+        return sw::host_entry<T>(A);                                          \
+    }
+
+#define SW_DEFINE_3D_CD(SFX, T)                                               \
+    extern "C" double simwave_forward_3d_cd_##SFX(                            \
+        T* u, T* velocity, T* damp, T* wavelet, size_t wavelet_size,          \
+        size_t wavelet_count, T* coeff, size_t* boundary_conditions,          \
+        size_t* src_points_interval, size_t src_points_interval_size,         \
+        T* src_points_values, size_t src_points_values_size,                  \
+        size_t* src_points_values_offset, size_t* rec_points_interval,        \
+        size_t rec_points_interval_size, T* rec_points_values,                \
+        size_t rec_points_values_size, size_t* rec_points_values_offset,      \
+        T* receivers, size_t num_sources, size_t num_receivers, size_t nz,    \
+        size_t nx, size_t ny, T dz, T dx, T dy, size_t saving_stride, T dt,   \
+        size_t begin_timestep, size_t end_timestep, size_t space_order,       \
+        size_t num_snapshots) {                                               \
+        HostArgs<T> A{};                                                      \
+        SW_HOST_ARGS_COMMON(T)                                                \
+        A.dim = 3; A.vd = false; A.den = nullptr; A.c2 = coeff;               \
+        A.c1 = nullptr; A.nz = nz; A.nx = nx; A.ny = ny; A.dz = dz;           \
+        A.dx = dx; A.dy = dy;                                                 \
+        return sw::host_entry<T>(A);                                          \
+    }
+
+#define SW_DEFINE_3D_VD(SFX, T)                                               \
+    extern "C" double simwave_forward_3d_vd_##SFX(                            \
+        T* u, T* velocity, T* density, T* damp, T* wavelet,                   \
+        size_t wavelet_size, size_t wavelet_count, T* coeff_order2,           \
+        T* coeff_order1, size_t* boundary_conditions,                         \
+        size_t* src_points_interval, size_t src_points_interval_size,         \
+        T* src_points_values, size_t src_points_values_size,                  \
+        size_t* src_points_values_offset, size_t* rec_points_interval,        \
+        size_t rec_points_interval_size, T* rec_points_values,                \
+        size_t rec_points_values_size, size_t* rec_points_values_offset,      \
+        T* receivers, size_t num_sources, size_t num_receivers, size_t nz,    \
+        size_t nx, size_t ny, T dz, T dx, T dy, size_t saving_stride, T dt,   \
+        size_t begin_timestep, size_t end_timestep, size_t space_order,       \
+        size_t num_snapshots) {                                               \
+        HostArgs<T> A{};                                                      \
+        SW_HOST_ARGS_COMMON(T)                                                \
+        A.dim = 3; A.vd = true; A.den = density; A.c2 = coeff_order2;         \
+        A.c1 = coeff_order1; A.nz = nz; A.nx = nx; A.ny = ny; A.dz = dz;      \
+        A.dx = dx; A.dy = dy;                                                 \
+        return sw::host_entry<T>(A);                                          \
+    }
+
+SW_DEFINE_2D_CD(f32, float)
+SW_DEFINE_2D_CD(f64, double)
+SW_DEFINE_2D_VD(f32, float)
+SW_DEFINE_2D_VD(f64, double)
+SW_DEFINE_3D_CD(f32, float)
+SW_DEFINE_3D_CD(f64, double)
+SW_DEFINE_3D_VD(f32, float)
+SW_DEFINE_3D_VD(f64, double)
+
+extern "C" const char* simwave_last_error(void) { return sw::g_last_error.c_str(); }
+
+extern "C" int simwave_forward_device(const simwave_problem* problem, void* stream) {
+    try {
+        sw::g_last_error.clear();
+        if (!problem) sw::fail(SIMWAVE_E_ARGUMENT, "null problem");
+        if (problem->precision == 4)
+            return sw::device_forward<float>(problem, (cudaStream_t)stream);
+        if (problem->precision == 8)
+            return sw::device_forward<double>(problem, (cudaStream_t)stream);
+        sw::fail(SIMWAVE_E_ARGUMENT, "precision must be 4 or 8");
+    } catch (const sw::Failure& f) {
+        sw::g_last_error = f.message;
+        return f.code;
+    } catch (const std::exception& e) {
+        sw::g_last_error = e.what();
+        return SIMWAVE_E_ARGUMENT;
+    }
+}
+
+extern "C" int simwave_last_stats(simwave_stats* out) {
+    if (!out) return SIMWAVE_E_ARGUMENT;
+    *out = sw::g_last_stats;
+    return SIMWAVE_OK;
+}
+
+extern "C" int simwave_layout(size_t fastest_extent, int space_order,
+                              int precision, size_t* pitch, size_t* lead) {
+    if (!pitch || !lead || (precision != 4 && precision != 8) ||
+        space_order < 2 || space_order > 20 || space_order % 2)
+        return SIMWAVE_E_ARGUMENT;
+    sw::choose_layout(fastest_extent, space_order / 2, precision, pitch, lead);
+    return SIMWAVE_OK;
+}

@@ -1,0 +1,147 @@
+"""GPU properties: the reference's snapshot-invariance and golden-solution
+tests through the drop-in Solver, and size-independent identities checked at
+the full 3D benchmark size (472^3 extended grid, order 8, variable density).
+"""
+import numpy as np
+import pytest
+
+import simwave_gb300 as sw
+from _cases import fixture_kwargs, load_fixture, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+# ---- reference tests/test_u_saving.py: last snapshot identical for every
+# saving stride (configurations chosen so that the stride padding never
+# changes the number of time steps)
+
+def _saving_2d(density, stride):
+    vel = np.zeros((512, 512), dtype=np.float32)
+    vel[:] = 1500.0
+    vel[250:] = 3000.0
+    den = np.full((512, 512), 5, dtype=np.float32) if density else None
+    sm = sw.SpaceModel((0, 5120, 0, 5120), (10, 10), vel, den, space_order=4)
+    sm.config_boundary(damping_length=0, boundary_condition=(
+        "null_neumann", "null_dirichlet", "none", "null_dirichlet"),
+        damping_polynomial_degree=3, damping_alpha=0.001)
+    tm = sw.TimeModel(space_model=sm, tf=1.0, saving_stride=stride)
+    src = sw.Source(sm, coordinates=[(2560, 2560)], window_radius=4)
+    rec = sw.Receiver(sm, coordinates=[(2560, i) for i in range(0, 5120, 10)],
+                      window_radius=4)
+    solver = sw.Solver(sm, tm, src, rec, sw.RickerWavelet(10.0, tm))
+    return solver.forward()[0][-1]
+
+
+def _saving_3d(density, stride):
+    vel = np.zeros((100, 100, 100), dtype=np.float32)
+    vel[:] = 1500.0
+    vel[50:] = 2000.0
+    den = np.full((100, 100, 100), 5, dtype=np.float32) if density else None
+    sm = sw.SpaceModel((0, 1000, 0, 1000, 0, 1000), (10, 10, 10), vel, den,
+                       space_order=4)
+    sm.config_boundary(damping_length=0, boundary_condition=(
+        "null_neumann", "null_dirichlet", "none", "null_dirichlet",
+        "null_neumann", "null_dirichlet"),
+        damping_polynomial_degree=3, damping_alpha=0.001)
+    tm = sw.TimeModel(space_model=sm, tf=0.3, saving_stride=stride)
+    src = sw.Source(sm, coordinates=[(500, 495, 505)], window_radius=4)
+    rec = sw.Receiver(sm, coordinates=[(500, 495, 505)], window_radius=4)
+    solver = sw.Solver(sm, tm, src, rec, sw.RickerWavelet(15.0, tm))
+    return solver.forward()[0][-1]
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_last_snapshot_independent_of_stride_2d(density):
+    base = _saving_2d(density, 0)
+    for stride in (1, 2, 3, 4, 5):
+        assert np.array_equal(_saving_2d(density, stride), base), stride
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_last_snapshot_independent_of_stride_3d(density):
+    base = _saving_3d(density, 0)
+    for stride in (1, 2, 3, 4, 5):
+        assert np.array_equal(_saving_3d(density, stride), base), stride
+
+
+# ---- reference tests/test_solution.py (2D): Solver.forward() against the
+# reference's golden wavefield, atol 1e-5 as in the reference test
+
+@pytest.mark.parametrize("order", [2, 8])
+def test_solution_2d_golden(order):
+    vel = np.zeros((500, 500), dtype=np.float32)
+    vel[:] = 1500.0
+    vel[250:] = 2000.0
+    sm = sw.SpaceModel((0, 5000, 0, 5000), (10, 10), vel, space_order=order)
+    sm.config_boundary(damping_length=100, boundary_condition=(
+        "null_neumann", "null_dirichlet", "none", "null_dirichlet"),
+        damping_polynomial_degree=3, damping_alpha=0.001)
+    tm = sw.TimeModel(space_model=sm, tf=1.0, saving_stride=0)
+    src = sw.Source(sm, coordinates=[(2500, 2500)], window_radius=1)
+    rec = sw.Receiver(sm, coordinates=[(2500, 2500)], window_radius=1)
+    solver = sw.Solver(sm, tm, src, rec, sw.RickerWavelet(10.0, tm))
+    u, recv = solver.forward()
+    meta, ref = load_fixture("solution_2d_so{}".format(order))
+    halo = order // 2
+    u_ref = ref["u_full"][:, halo:-halo, halo:-halo]
+    assert u.shape == u_ref.shape
+    assert np.allclose(u, u_ref, atol=1e-5)
+    assert rel_l2(u, u_ref) < 1e-4
+    assert rel_l2(recv, ref["shot_record"]) < 1e-4
+
+
+# ---- full-size identities (3D VD order 8, 472^3 extended grid)
+
+@pytest.fixture(scope="module")
+def big_problem():
+    import bench
+    kw = bench.config2_arguments(timesteps=61)
+    return kw
+
+
+def test_full_size_source_linearity(big_problem):
+    """Scaling the wavelet by 2 scales every output by exactly 2."""
+    import torch
+    from simwave_gb300.device import DeviceProblem
+    kw = dict(big_problem)
+    dp = DeviceProblem(kw)
+    dp.run()
+    u1 = dp.u.clone()
+    r1 = dp.receivers.clone()
+    kw2 = dict(kw)
+    kw2["wavelet"] = kw["wavelet"] * kw["wavelet"].dtype.type(2)
+    dp2 = DeviceProblem(kw2)
+    dp2.run()
+    torch.cuda.synchronize()
+    assert torch.equal(dp2.u, 2 * u1)
+    assert torch.equal(dp2.receivers, 2 * r1)
+    assert float(u1.abs().max()) > 0
+
+
+def test_full_size_stride_invariance(big_problem):
+    """The level every stride keeps last is identical for strides 0 and 4."""
+    import torch
+    from simwave_gb300.device import DeviceProblem
+    kw0 = dict(big_problem)
+    T = kw0["end_timestep"]
+    kw0["saving_stride"] = 0
+    kw0["num_snapshots"] = 3
+    kw0["u_full"] = np.zeros((3,) + big_problem["u_full"].shape[1:],
+                             dtype=big_problem["u_full"].dtype)
+    dp0 = DeviceProblem(kw0)
+    dp0.run()
+    last0 = dp0.u[T % 3].clone()
+    rec0 = dp0.receivers.clone()
+    del dp0
+    kw4 = dict(big_problem)
+    kw4["saving_stride"] = 4
+    nsnap = len(range(0, T, 4))
+    kw4["num_snapshots"] = nsnap + 2
+    kw4["u_full"] = np.zeros((nsnap + 2,) + kw0["u_full"].shape[1:],
+                             dtype=kw0["u_full"].dtype)
+    assert (T - 1) % 4 == 0
+    dp4 = DeviceProblem(kw4)
+    dp4.run()
+    torch.cuda.synchronize()
+    assert torch.equal(dp4.u[nsnap], last0)
+    assert torch.equal(dp4.receivers, rec0)
