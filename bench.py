@@ -93,6 +93,9 @@ def config2_arguments(timesteps=None, n=384, stride=50):
     kw = solver.forward_arguments()
     if timesteps is not None and timesteps < kw["end_timestep"]:
         T = int(timesteps)
+        if stride > 1 and T % stride != 1:
+            raise ValueError("a run with saving stride %d needs T %% stride == 1"
+                             " (T = %d)" % (stride, T))
         kw["end_timestep"] = T
         kw["wavelet"] = np.ascontiguousarray(kw["wavelet"][:T])
         kw["wavelet_size"] = T
@@ -176,13 +179,13 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU checker timing (bounded sample)
 
-def cpu_sample(steps, threads=None):
+def cpu_sample(steps, threads=None, n=384):
     """Gpts/s of the C restatement on `steps` time steps of the workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     threads = threads or os.cpu_count()
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    kw = config2_arguments(timesteps=steps, stride=0)
+    kw = config2_arguments(timesteps=steps, stride=0, n=n)
     pts, updates = interior_updates(kw)
     _, _, secs = oracle.forward("port", x_stride="layout", **kw)
     return updates / secs / 1e9, secs, threads
@@ -263,6 +266,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=384,
+                    help="model points per axis (default 384)")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -276,7 +281,7 @@ def main():
     from simwave_gb300.device import DeviceProblem
 
     torch.cuda.set_device(local)
-    kw = config2_arguments(timesteps=args.timesteps)
+    kw = config2_arguments(timesteps=args.timesteps, n=args.n)
     pts, updates = interior_updates(kw)
     dp = DeviceProblem(kw, device="cuda:%d" % local)
     stream = torch.cuda.current_stream()
@@ -338,7 +343,7 @@ def main():
     mw = Middleware()
     import contextlib
     import io
-    for i in range(args.e2e_steps + 1):
+    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         k = dict(kw)
         k["u_full"] = np.zeros_like(kw["u_full"])
         k["shot_record"] = np.zeros_like(kw["shot_record"])
@@ -352,12 +357,17 @@ def main():
             s = _lib.last_stats()
             h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
             launches_e2e = s["kernel_launches"]
-    e2e_total = max_over_ranks(float(np.sum(e2e_ms)), world)
-    e2e_value = updates * world / (e2e_total / len(e2e_ms) / 1e3) / 1e9
+    e2e = None
+    if e2e_ms:
+        e2e_total = max_over_ranks(float(np.sum(e2e_ms)), world)
+        e2e_value = updates * world / (e2e_total / len(e2e_ms) / 1e3) / 1e9
+        e2e = {"value": round(e2e_value, 3), "unit": "Gpts/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": round(e2e_total / len(e2e_ms), 3)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, secs, threads = cpu_sample(args.cpu_steps)
+        rate, secs, threads = cpu_sample(args.cpu_steps, n=args.n)
         cpu = {"value": round(rate, 4), "unit": "Gpts/s", "cores": threads,
                "kind": "port",
                "sample": "%d of 1201 time steps on the full 472^3 grid "
@@ -370,7 +380,8 @@ def main():
             "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "3d_vd_so8_472cube_T%d_s50" % kw["end_timestep"],
+            "config": {"workload": "3d_vd_so8_%dcube_T%d_s50" % (
+                           kw["velocity_model"].shape[0], kw["end_timestep"]),
                        "grid": list(kw["velocity_model"].shape),
                        "timesteps": kw["end_timestep"],
                        "updates_per_step": updates,
@@ -382,10 +393,7 @@ def main():
                          "peak_source": peak_src,
                          "kernel_ms": round(stencil_ms, 4),
                          "bytes_per_launch": bytes_per_launch},
-            "e2e": {"value": round(e2e_value, 3), "unit": "Gpts/s",
-                    "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": round(e2e_total / len(e2e_ms), 3)},
+            "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clock_info,
             "cpu_baseline": cpu,

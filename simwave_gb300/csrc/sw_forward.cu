@@ -5,6 +5,7 @@
 // error reporting. Kernels live in sw_kernels.cuh (generic) and
 // sw_stencil_tiled.cu (tiled fast path).
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -151,6 +152,7 @@ struct Buffer {
         bytes = 0;
         if (n == 0) return nullptr;
         SW_CUDA(cudaMalloc(&ptr, n));
+        SW_CUDA(cudaMemset(ptr, 0, n));  // row padding is never written
         bytes = n;
         return ptr;
     }
@@ -207,26 +209,33 @@ static Weights<T> make_weights(const T* c2, const T* c1, int r, double dz,
     Weights<T> W;
     std::memset(&W, 0, sizeof(W));
     const double h[3] = {dz, dx, dy};
-    for (int a = 0; a < 3; a++) {
-        const double h2 = h[a] * h[a];
-        for (int k = 0; k <= r; k++) W.c2[a][k] = (T)((double)c2[k] / h2);
-        W.s1[a] = (T)(1.0 / (4.0 * h2));
+    for (int k = 0; k <= r; k++) {
+        W.c2[k] = c2[k];
+        W.c1[k] = c1 ? c1[k] : T(0);
     }
-    for (int k = 0; k <= r; k++) W.c1[k] = c1 ? c1[k] : T(0);
+    for (int a = 0; a < 3; a++) {
+        // h^2 as the reference forms it: in the model precision
+        const T h2 = (T)h[a] * (T)h[a];
+        W.ih2[a] = (T)(1.0 / (double)h2);
+        W.s1[a] = (T)(1.0 / (4.0 * (double)h2));
+    }
     return W;
 }
 
 template <typename T, int DIM, bool VD>
-static void launch_stencil(const Run<T>& R, T* un, const T* uc, const T* up,
-                           cudaStream_t st, int* variant) {
+static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
+                           const T* uc, const T* up, cudaStream_t st,
+                           int* variant) {
     const Layout& L = R.L;
     const T dt2 = R.dt * R.dt;
-    if (tiled_supported<T, DIM, VD>(L)) {
-        launch_tiled<T, DIM, VD>(un, uc, up, R.vel, R.den, R.damp, L, R.W,
-                                 R.dt, dt2, st);
-        *variant = 1;
-        SW_LAUNCHED("stencil_tiled");
-        return;
+    if constexpr (std::is_same<T, float>::value && DIM == 3) {
+        if (tctx.ok) {
+            tiled_launch(tctx, VD, un, uc, up, R.vel, R.den, R.damp, L, R.W,
+                         R.dt, dt2, st);
+            *variant = 1;
+            SW_LAUNCHED("stencil3d_tiled");
+            return;
+        }
     }
     const int r = L.r;
     dim3 block(32, 8, 1);
@@ -239,6 +248,44 @@ static void launch_stencil(const Run<T>& R, T* un, const T* uc, const T* up,
     SW_LAUNCHED("stencil_generic");
 }
 
+// Per-device words the kernels report into: [0..5] zero box, [6] box check,
+// [7] error code of bounded waits. Allocated once per device.
+static int* device_words() {
+    static std::mutex m;
+    static std::map<int, int*> words;
+    int dev = 0;
+    SW_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(m);
+    int*& w = words[dev];
+    if (!w) {
+        SW_CUDA(cudaMalloc(&w, 16 * sizeof(int)));
+        SW_CUDA(cudaMemset(w, 0, 16 * sizeof(int)));
+    }
+    return w;
+}
+
+// Tiled-kernel context of one run (float32 3D only).
+template <typename T>
+static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
+    TiledContext ctx;
+    if constexpr (std::is_same<T, float>::value) {
+        if (R.L.dim != 3 || (R.flags & SIMWAVE_FLAG_GENERIC_KERNEL)) return ctx;
+        if (!tiled_prepare(ctx, R.L, R.vd, R.u, (long long)R.nslots,
+                           (long long)R.L.slot, R.den))
+            return ctx;
+        int* words = device_words();
+        find_zero_box(R.damp, R.L, words, st);
+        SW_LAUNCHED("find_zero_box");
+        int box[7];
+        SW_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
+        SW_CUDA(cudaStreamSynchronize(st));
+        const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2] && box[5] > box[4];
+        for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
+        ctx.err = words + 7;
+    }
+    return ctx;
+}
+
 template <typename T, int DIM, bool VD>
 static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
                       simwave_stats& stats, std::vector<cudaEvent_t>* ev) {
@@ -248,13 +295,14 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
     int phases[3], nphase = 0;
     if (DIM == 3) { phases[0] = 2; phases[1] = 1; phases[2] = 0; nphase = 3; }
     else { phases[0] = 1; phases[1] = 0; nphase = 2; }
+    const TiledContext tctx = prepare_tiled<T>(R, st);
     for (size_t i = 0; i < S.steps.size(); i++) {
         const size_t n = R.begin + i;
         T* un = R.u + (size_t)S.steps[i].next * L.slot;
         const T* uc = R.u + (size_t)S.steps[i].cur * L.slot;
         const T* up = R.u + (size_t)S.steps[i].prev * L.slot;
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i], st));
-        launch_stencil<T, DIM, VD>(R, un, uc, up, st, &stats.stencil_variant);
+        launch_stencil<T, DIM, VD>(R, tctx, un, uc, up, st, &stats.stencil_variant);
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i + 1], st));
         stats.stencil_launches++;
         stats.kernel_launches++;
@@ -295,6 +343,19 @@ static void dispatch_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
     else if (R.L.dim == 2) run_steps<T, 2, true>(R, S, st, stats, ev);
     else if (!R.vd) run_steps<T, 3, false>(R, S, st, stats, ev);
     else run_steps<T, 3, true>(R, S, st, stats, ev);
+}
+
+// Reads and clears the bounded-wait error word (after the stream drained).
+static void check_device_words(cudaStream_t st) {
+    int* words = device_words();
+    int code = 0;
+    SW_CUDA(cudaMemcpyAsync(&code, words + 7, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SW_CUDA(cudaStreamSynchronize(st));
+    if (code) {
+        SW_CUDA(cudaMemsetAsync(words + 7, 0, sizeof(int), st));
+        SW_CUDA(cudaStreamSynchronize(st));
+        fail(code, "a device wait gave up (bounded mbarrier wait expired)");
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -511,6 +572,7 @@ static double host_forward(const HostArgs<T>& A) {
         d2h += rec_rows * A.nrec * sizeof(T);
     }
     SW_CUDA(cudaStreamSynchronize(st));
+    check_device_words(st);
     const double secs =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     stats.seconds = secs;
@@ -671,6 +733,7 @@ static int device_forward(const simwave_problem* P, cudaStream_t st) {
     }
     if (ev) {
         SW_CUDA(cudaStreamSynchronize(st));
+        check_device_words(st);
         double ms = 0;
         for (size_t i = 0; i < S.steps.size(); i++) {
             float t = 0;
@@ -819,6 +882,18 @@ extern "C" int simwave_forward_device(const simwave_problem* problem, void* stre
     } catch (const std::exception& e) {
         sw::g_last_error = e.what();
         return SIMWAVE_E_ARGUMENT;
+    }
+}
+
+extern "C" int simwave_device_status(void* stream) {
+    try {
+        sw::g_last_error.clear();
+        SW_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        sw::check_device_words((cudaStream_t)stream);
+        return SIMWAVE_OK;
+    } catch (const sw::Failure& f) {
+        sw::g_last_error = f.message;
+        return f.code;
     }
 }
 

@@ -33,10 +33,13 @@ __device__ __forceinline__ T leapfrog(T lap, T vel, T damp, T ucur, T uprev,
 
 // ---- generic stencil: one thread per interior point, runtime radius ------
 // Grid: x -> fastest axis, y -> middle axis, z -> slowest axis (3D).
+// `un` and `up` may be the same slot: with a saving stride > 1 the reference
+// writes level n+1 over level n-1 (constant_density/2d/wave.c:509-513); each
+// point reads its own previous value before writing it.
 template <typename T, int DIM, bool VD>
 __global__ void __launch_bounds__(256)
-stencil_generic(T* __restrict__ un, const T* __restrict__ uc,
-                const T* __restrict__ up, const T* __restrict__ vel,
+stencil_generic(T* un, const T* __restrict__ uc,
+                const T* up, const T* __restrict__ vel,
                 const T* __restrict__ den, const T* __restrict__ damp,
                 Layout L, Weights<T> W, T dt, T dt2) {
     const int r = L.r;
@@ -50,14 +53,13 @@ stencil_generic(T* __restrict__ un, const T* __restrict__ uc,
     const int am = DIM == 3 ? 1 : 0;
     const long long sm = L.pitch, ss = L.plane;
     const T u0 = uc[p];
-    T lap_f = W.c2[af][0] * u0, lap_m = W.c2[am][0] * u0, lap_s = 0;
-    if (DIM == 3) lap_s = W.c2[0][0] * u0;
+    T lap_f = W.c2[0] * u0, lap_m = W.c2[0] * u0, lap_s = W.c2[0] * u0;
     T gu_f = 0, gu_m = 0, gu_s = 0, gr_f = 0, gr_m = 0, gr_s = 0;
     for (int k = 1; k <= r; k++) {
         const T fp = uc[p + k], fm = uc[p - k];
         const T mp = uc[p + k * sm], mm = uc[p - k * sm];
-        lap_f += W.c2[af][k] * (fp + fm);
-        lap_m += W.c2[am][k] * (mp + mm);
+        lap_f += W.c2[k] * (fp + fm);
+        lap_m += W.c2[k] * (mp + mm);
         if (VD) {
             gu_f += W.c1[k] * (fp - fm);
             gu_m += W.c1[k] * (mp - mm);
@@ -66,14 +68,16 @@ stencil_generic(T* __restrict__ un, const T* __restrict__ uc,
         }
         if (DIM == 3) {
             const T sp = uc[p + k * ss], sq = uc[p - k * ss];
-            lap_s += W.c2[0][k] * (sp + sq);
+            lap_s += W.c2[k] * (sp + sq);
             if (VD) {
                 gu_s += W.c1[k] * (sp - sq);
                 gr_s += W.c1[k] * (den[p + k * ss] - den[p - k * ss]);
             }
         }
     }
-    T lap = lap_f + lap_m + lap_s;
+    // axis order of the reference's sum: y, x, z (3D); x, z (2D)
+    T lap = lap_f * W.ih2[af] + lap_m * W.ih2[am];
+    if (DIM == 3) lap += lap_s * W.ih2[0];
     if (VD) {
         T cross = gu_f * gr_f * W.s1[af] + gu_m * gr_m * W.s1[am];
         if (DIM == 3) cross += gu_s * gr_s * W.s1[0];

@@ -1,18 +1,36 @@
-// sw_tiled.h -- entry points of the tiled stencil kernels (sw_stencil_tiled.cu).
+// sw_tiled.h -- tiled 3D float32 stencil (sw_stencil_tiled.cu).
 #pragma once
 
 #include "sw_common.cuh"
 
 namespace sw {
 
-// True when the tiled kernel handles this (precision, dimension, density,
-// layout); otherwise the generic kernel runs.
-template <typename T, int DIM, bool VD>
-bool tiled_supported(const Layout& L);
+// Per-run state of the tiled kernel: TMA descriptors of the wavefield slots
+// and of the density, the box where the damping mask is zero, and the device
+// error word that bounded waits set on expiry.
+struct TiledContext {
+    bool ok = false;
+    alignas(64) unsigned char map_u[128];
+    alignas(64) unsigned char map_rho[128];
+    const float* u_base = nullptr;
+    long long slot_stride = 0;
+    int zero_box[6] = {0, 0, 0, 0, 0, 0};  // z0, z1, x0, x1, y0, y1 (empty)
+    int* err = nullptr;
+};
 
-template <typename T, int DIM, bool VD>
-void launch_tiled(T* un, const T* uc, const T* up, const T* vel, const T* den,
-                  const T* damp, const Layout& L, const Weights<T>& W, T dt,
-                  T dt2, cudaStream_t st);
+// Encodes the descriptors; false when the layout or alignment does not suit
+// the tiled kernel (the generic kernel then runs).
+bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
+                   long long nslots, long long slot_stride, const float* den);
+
+void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc,
+                  const float* up, const float* vel, const float* den,
+                  const float* damp, const Layout& L, const Weights<float>& W,
+                  float dt, float dt2, cudaStream_t st);
+
+// Largest box around the grid centre (interior indices) where `damp` is zero,
+// found and verified on the device; writes {z0, z1, x0, x1, y0, y1} into the
+// device array `box` (7 ints: the 6 bounds and a verification word).
+void find_zero_box(const float* damp, const Layout& L, int* box, cudaStream_t st);
 
 }  // namespace sw

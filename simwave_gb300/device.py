@@ -50,6 +50,7 @@ class Problem(ctypes.Structure):
 
 FLAG_TIME_KERNELS = 1
 FLAG_WINDOWS_CHECKED = 2
+FLAG_GENERIC_KERNEL = 4
 
 
 def layout(fastest_extent, space_order, precision):
@@ -210,11 +211,14 @@ class DeviceProblem:
         self._u.zero_()
         self.receivers.zero_()
 
-    def run(self, stream=None, time_kernels=False):
-        """Launch the forward loop on ``stream`` (torch stream or None)."""
+    def run(self, stream=None, time_kernels=False, generic=False):
+        """Launch the forward loop on ``stream`` (torch stream or None).
+
+        ``generic`` forces the one-thread-per-point stencil kernel."""
         lib = _lib.load()
         self.problem.flags = FLAG_WINDOWS_CHECKED | (
-            FLAG_TIME_KERNELS if time_kernels else 0)
+            FLAG_TIME_KERNELS if time_kernels else 0) | (
+            FLAG_GENERIC_KERNEL if generic else 0)
         handle = None
         if stream is not None:
             handle = ctypes.c_void_p(stream.cuda_stream)
@@ -225,6 +229,14 @@ class DeviceProblem:
             raise RuntimeError("simwave_forward_device failed ({}): {}".format(
                 status, _lib.last_error()))
         return _lib.last_stats()
+
+    def status(self, stream=None):
+        """Wait for the stream and raise if a device-side wait expired."""
+        lib = _lib.load()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        status = lib.simwave_device_status(ctypes.c_void_p(s.cuda_stream))
+        if status != 0:
+            raise RuntimeError("device status {}: {}".format(status, _lib.last_error()))
 
     def u_full_numpy(self):
         return self.u.cpu().numpy()

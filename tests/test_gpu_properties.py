@@ -11,9 +11,10 @@ from _cases import fixture_kwargs, load_fixture, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-# ---- reference tests/test_u_saving.py: last snapshot identical for every
-# saving stride (configurations chosen so that the stride padding never
-# changes the number of time steps)
+# ---- reference tests/test_u_saving.py:1-209: the last snapshot is identical
+# for every saving stride (configurations where the stride padding never
+# changes the number of time steps: 2D T = 491 for strides 0, 1, 2, 5;
+# 3D T = 121 for strides 0..5)
 
 def _saving_2d(density, stride):
     vel = np.zeros((512, 512), dtype=np.float32)
@@ -35,17 +36,17 @@ def _saving_2d(density, stride):
 def _saving_3d(density, stride):
     vel = np.zeros((100, 100, 100), dtype=np.float32)
     vel[:] = 1500.0
-    vel[50:] = 2000.0
     den = np.full((100, 100, 100), 5, dtype=np.float32) if density else None
     sm = sw.SpaceModel((0, 1000, 0, 1000, 0, 1000), (10, 10, 10), vel, den,
                        space_order=4)
     sm.config_boundary(damping_length=0, boundary_condition=(
-        "null_neumann", "null_dirichlet", "none", "null_dirichlet",
-        "null_neumann", "null_dirichlet"),
+        "null_neumann", "null_dirichlet", "null_dirichlet", "null_dirichlet",
+        "null_dirichlet", "null_dirichlet"),
         damping_polynomial_degree=3, damping_alpha=0.001)
-    tm = sw.TimeModel(space_model=sm, tf=0.3, saving_stride=stride)
-    src = sw.Source(sm, coordinates=[(500, 495, 505)], window_radius=4)
-    rec = sw.Receiver(sm, coordinates=[(500, 495, 505)], window_radius=4)
+    tm = sw.TimeModel(space_model=sm, tf=0.4, saving_stride=stride)
+    src = sw.Source(sm, coordinates=[(500, 500, 500)], window_radius=4)
+    rec = sw.Receiver(sm, coordinates=[(500, 500, i) for i in range(0, 1000, 10)],
+                      window_radius=4)
     solver = sw.Solver(sm, tm, src, rec, sw.RickerWavelet(15.0, tm))
     return solver.forward()[0][-1]
 
@@ -53,7 +54,7 @@ def _saving_3d(density, stride):
 @pytest.mark.parametrize("density", [False, True])
 def test_last_snapshot_independent_of_stride_2d(density):
     base = _saving_2d(density, 0)
-    for stride in (1, 2, 3, 4, 5):
+    for stride in (1, 2, 5):
         assert np.array_equal(_saving_2d(density, stride), base), stride
 
 
@@ -95,8 +96,7 @@ def test_solution_2d_golden(order):
 @pytest.fixture(scope="module")
 def big_problem():
     import bench
-    kw = bench.config2_arguments(timesteps=61)
-    return kw
+    return bench.config2_arguments(timesteps=61, stride=4)
 
 
 def test_full_size_source_linearity(big_problem):
@@ -104,6 +104,10 @@ def test_full_size_source_linearity(big_problem):
     import torch
     from simwave_gb300.device import DeviceProblem
     kw = dict(big_problem)
+    kw["saving_stride"] = 0
+    kw["num_snapshots"] = 3
+    kw["u_full"] = np.zeros((3,) + big_problem["u_full"].shape[1:],
+                            dtype=big_problem["u_full"].dtype)
     dp = DeviceProblem(kw)
     dp.run()
     u1 = dp.u.clone()
