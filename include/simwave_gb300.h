@@ -243,6 +243,16 @@ int simwave_layout(size_t fastest_extent, int space_order, int precision,
  * No reference counterpart: the reference allocates and copies per call. */
 int simwave_forward_device(const simwave_problem *problem, void *stream);
 
+/* Stencil kernel selection for the float32 3D path (process-wide).
+ * AUTO picks per order and density; the others force one variant (tuning
+ * and tests). Returns SIMWAVE_OK or SIMWAVE_E_ARGUMENT.
+ * No reference counterpart. */
+#define SIMWAVE_POLICY_AUTO 0
+#define SIMWAVE_POLICY_SCALAR_TILED 1   /* one y point per thread */
+#define SIMWAVE_POLICY_VEC_2CTA 2       /* float4 along y, 2 CTAs per SM */
+#define SIMWAVE_POLICY_VEC_1CTA 3       /* float4 along y, 1 CTA per SM */
+int simwave_set_kernel_policy(int policy);
+
 /* Wait for `stream` and report device-side failures of the forward calls
  * enqueued on it (a bounded wait that expired: SIMWAVE_E_TIMEOUT). Clears
  * the recorded status. No reference counterpart. */

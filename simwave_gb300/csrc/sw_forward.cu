@@ -897,6 +897,13 @@ extern "C" int simwave_device_status(void* stream) {
     }
 }
 
+extern "C" int simwave_set_kernel_policy(int policy) {
+    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_1CTA)
+        return SIMWAVE_E_ARGUMENT;
+    sw::set_kernel_policy(policy);
+    return SIMWAVE_OK;
+}
+
 extern "C" int simwave_last_stats(simwave_stats* out) {
     if (!out) return SIMWAVE_E_ARGUMENT;
     *out = sw::g_last_stats;

@@ -292,6 +292,253 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
     }
 }
 
+
+// ---- vectorised kernel: 4 consecutive y points per thread (orders <= 8) ----
+//
+// Warp w of the CTA owns x row R + 8*blockIdx.y + w; lane l owns y points
+// y0 .. y0+3, y0 = R + 128*blockIdx.x + 4l. Global traffic is float4 per
+// thread; the y window (4 + 2*HY values) and the x neighbours come from the
+// TMA tile as 16-byte shared loads; z neighbours from float4 register queues.
+
+__device__ __forceinline__ float4 f4(float a) { return make_float4(a, a, a, a); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ float4 sub4(float4 a, float4 b) {
+    return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+__device__ __forceinline__ float4 fma4(float c, float4 a, float4 acc) {
+    return make_float4(fmaf(c, a.x, acc.x), fmaf(c, a.y, acc.y), fmaf(c, a.z, acc.z),
+                       fmaf(c, a.w, acc.w));
+}
+__device__ __forceinline__ float4 mul4(float c, float4 a) {
+    return make_float4(c * a.x, c * a.y, c * a.z, c * a.w);
+}
+__device__ __forceinline__ float comp(const float4& a, int v) {
+    return v == 0 ? a.x : (v == 1 ? a.y : (v == 2 ? a.z : a.w));
+}
+__device__ __forceinline__ void set_comp(float4& a, int v, float x) {
+    if (v == 0) a.x = x; else if (v == 1) a.y = x; else if (v == 2) a.z = x; else a.w = x;
+}
+
+// float4 load of points y0..y0+3 of a row; partial chunks load what exists
+// in memory (the row is never the last of its allocation) and are masked at
+// the store.
+__device__ __forceinline__ float4 ld4(const float* p, bool any) {
+    return any ? __ldg(reinterpret_cast<const float4*>(p)) : f4(0.f);
+}
+
+template <int R>
+struct VecTile {
+    static constexpr int HY = round4(R);
+    static constexpr int TW = 128 + 2 * HY;  // floats per tile row
+    static constexpr int TH = kWarps + 2 * R;
+    static constexpr int ELEMS = TW * TH;
+    static constexpr int BYTES = ELEMS * 4;
+    static constexpr int STRIDE = (ELEMS + 31) & ~31;
+    static constexpr int NC = (2 * HY) / 4 + 1;  // float4 chunks of a y window
+};
+
+template <int R, bool VD, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
+               const __grid_constant__ CUtensorMap map_rho, float* un,
+               const float* __restrict__ uc, const float* up,
+               const float* __restrict__ vel, const float* __restrict__ den,
+               const float* __restrict__ damp, Layout L, Weights<float> Wt, float dt,
+               float dt2, int slot_cur, int zchunk, ZeroBox zb, int* __restrict__ err) {
+    using VT = VecTile<R>;
+    constexpr int HY = VT::HY, TW = VT::TW, NC = VT::NC;
+    constexpr int NF = VD ? 2 : 1;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* tiles = reinterpret_cast<float*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) unsigned long long bars[kStages];
+    if (*(volatile int*)err) return;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int yb = R + blockIdx.x * 128;
+    const int y0 = yb + 4 * lane;
+    const int x = R + blockIdx.y * kWarps + warp;
+    const int zbeg = R + blockIdx.z * zchunk;
+    const int zend = min(zbeg + zchunk, (int)L.nz - R);
+    if (zbeg >= zend) return;
+    const int ylim = (int)L.ny - R;
+    const bool any = x < (int)L.nx - R && y0 < ylim;
+    const bool full = any && y0 + 3 < ylim;
+    const int off = x * (int)L.pitch + (int)L.lead + y0;
+    const int col0 = (int)L.lead + yb - HY;
+    const int row0 = blockIdx.y * kWarps;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int plane, int stage) {
+        mbar_expect_tx(&bars[stage], NF * VT::BYTES);
+        tma_load_4d(tiles + stage * VT::STRIDE, &map_u, &bars[stage], col0, row0, plane,
+                    slot_cur);
+        if (VD)
+            tma_load_4d(tiles + (kStages + stage) * VT::STRIDE, &map_rho, &bars[stage], col0,
+                        row0, plane, 0);
+    };
+    int issued = 0;
+    if (threadIdx.x == 0)
+        for (; issued < kStages && zbeg + issued < zend; issued++) issue(zbeg + issued, issued);
+
+    float4 qu[2 * R + 1];
+    float4 qr[VD ? 2 * R + 1 : 1];
+#pragma unroll
+    for (int j = 0; j < 2 * R; j++) {
+        const long long pz = (long long)(zbeg - R + j) * L.plane + off;
+        qu[j] = ld4(uc + pz, any);
+        if (VD) qr[j] = ld4(den + pz, any);
+    }
+    float4 hu, hr = f4(0.f);
+    {
+        const long long pz = (long long)(zbeg + R) * L.plane + off;
+        hu = ld4(uc + pz, any);
+        if (VD) hr = ld4(den + pz, any);
+    }
+
+    const float c20 = Wt.c2[0];
+    int aborted_at = -1;
+    for (int z = zbeg; z < zend; z++) {
+        const int it = z - zbeg;
+        const int stage = it % kStages;
+        qu[2 * R] = hu;
+        if (VD) qr[2 * R] = hr;
+        if (z + 1 < zend) {
+            const long long pz = (long long)(z + 1 + R) * L.plane + off;
+            hu = ld4(uc + pz, any);
+            if (VD) hr = ld4(den + pz, any);
+        }
+        const long long pz = (long long)z * L.plane + off;
+        // u_prev with a plain load: it may be the slot this kernel writes
+        const float4 vprev = any ? *reinterpret_cast<const float4*>(up + pz) : f4(0.f);
+        const float4 vvel = ld4(vel + pz, any);
+        const bool inbox = z >= zb.z0 && z < zb.z1 && x >= zb.x0 && x < zb.x1 &&
+                           y0 >= zb.y0 && y0 + 3 < zb.y1;
+        const float4 vdamp = ld4(damp + pz, any && !inbox);
+
+        // z axis: register queues
+        const float4 u0 = qu[R];
+        float4 sdz = mul4(c20, u0), fuz = f4(0.f), frz = f4(0.f);
+#pragma unroll
+        for (int k = 1; k <= R; k++) {
+            sdz = fma4(Wt.c2[k], add4(qu[R + k], qu[R - k]), sdz);
+            if (VD) {
+                fuz = fma4(Wt.c1[k], sub4(qu[R + k], qu[R - k]), fuz);
+                frz = fma4(Wt.c1[k], sub4(qr[R + k], qr[R - k]), frz);
+            }
+        }
+
+        const bool ok = mbar_wait(&bars[stage], (unsigned)((it / kStages) & 1));
+        if (__syncthreads_or(!ok)) {
+            aborted_at = it;
+            break;
+        }
+        const float* tu = tiles + stage * VT::STRIDE + (warp + R) * TW + 4 * lane;
+        const float* tr = tiles + (kStages + stage) * VT::STRIDE + (warp + R) * TW + 4 * lane;
+
+        // x axis: rows x +- k of the tile, this thread's 4 columns
+        float4 sdx = mul4(c20, u0), fux = f4(0.f), frx = f4(0.f);
+#pragma unroll
+        for (int k = 1; k <= R; k++) {
+            const float4 a = *reinterpret_cast<const float4*>(tu + k * TW + HY);
+            const float4 b = *reinterpret_cast<const float4*>(tu - k * TW + HY);
+            sdx = fma4(Wt.c2[k], add4(a, b), sdx);
+            if (VD) {
+                fux = fma4(Wt.c1[k], sub4(a, b), fux);
+                const float4 ra = *reinterpret_cast<const float4*>(tr + k * TW + HY);
+                const float4 rb = *reinterpret_cast<const float4*>(tr - k * TW + HY);
+                frx = fma4(Wt.c1[k], sub4(ra, rb), frx);
+            }
+        }
+
+        // y axis: window of 4 + 2*HY values of this thread's row
+        float wu[4 * NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const float4 t = *reinterpret_cast<const float4*>(tu + 4 * c);
+            wu[4 * c] = t.x; wu[4 * c + 1] = t.y; wu[4 * c + 2] = t.z; wu[4 * c + 3] = t.w;
+        }
+        float4 sdy = mul4(c20, u0), fuy = f4(0.f), fry = f4(0.f);
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            float s = comp(sdy, v), g = 0.f;
+#pragma unroll
+            for (int k = 1; k <= R; k++) {
+                s = fmaf(Wt.c2[k], wu[HY + v + k] + wu[HY + v - k], s);
+                if (VD) g = fmaf(Wt.c1[k], wu[HY + v + k] - wu[HY + v - k], g);
+            }
+            set_comp(sdy, v, s);
+            set_comp(fuy, v, g);
+        }
+        if (VD) {
+            float wr[4 * NC];
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const float4 t = *reinterpret_cast<const float4*>(tr + 4 * c);
+                wr[4 * c] = t.x; wr[4 * c + 1] = t.y; wr[4 * c + 2] = t.z; wr[4 * c + 3] = t.w;
+            }
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                float g = 0.f;
+#pragma unroll
+                for (int k = 1; k <= R; k++)
+                    g = fmaf(Wt.c1[k], wr[HY + v + k] - wr[HY + v - k], g);
+                set_comp(fry, v, g);
+            }
+        }
+
+        // combine (reference order y, x, z) and update
+        float4 out;
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            float lap = comp(sdy, v) * Wt.ih2[2] + comp(sdx, v) * Wt.ih2[1];
+            lap = fmaf(comp(sdz, v), Wt.ih2[0], lap);
+            if (VD) {
+                float cross = comp(fuy, v) * comp(fry, v) * Wt.s1[2] +
+                              comp(fux, v) * comp(frx, v) * Wt.s1[1];
+                cross = fmaf(comp(fuz, v) * comp(frz, v), Wt.s1[0], cross);
+                lap -= __fdividef(cross, comp(qr[R], v));
+            }
+            const float vv = comp(vvel, v);
+            const float v2 = vv * vv;
+            const float q = comp(vdamp, v) * dt * v2 * 0.5f;
+            const float rden = __frcp_rn(1.f + q);
+            const float num = fmaf(-(1.f - q), comp(vprev, v), 2.f * comp(u0, v));
+            set_comp(out, v, fmaf(dt2 * v2, lap, num) * rden);
+        }
+        if (full) {
+            *reinterpret_cast<float4*>(un + pz) = out;
+        } else if (any) {
+#pragma unroll
+            for (int v = 0; v < 4; v++)
+                if (y0 + v < ylim) un[pz + v] = comp(out, v);
+        }
+
+        __syncthreads();
+        if (threadIdx.x == 0 && z + kStages < zend) {
+            issue(z + kStages, stage);
+            issued++;
+        }
+#pragma unroll
+        for (int j = 0; j < 2 * R; j++) {
+            qu[j] = qu[j + 1];
+            if (VD) qr[j] = qr[j + 1];
+        }
+    }
+    if (aborted_at >= 0 && threadIdx.x == 0) {
+        atomicExch(err, SIMWAVE_E_TIMEOUT);
+        for (int p = aborted_at; p < issued; p++)
+            mbar_wait(&bars[p % kStages], (unsigned)((p / kStages) & 1));
+    }
+}
+
 // ---- host side ---------------------------------------------------------------
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -339,6 +586,26 @@ DeviceInfo& device_info() {
     return d;
 }
 
+
+// z chunk length: fill the machine in whole waves, counting the 2R-plane
+// warm-up of every chunk as the cost of splitting.
+int choose_chunk(int ty, int tx, int nzi, int R, int per_sm) {
+    const long long slots = (long long)std::max(per_sm, 1) * device_info().sms;
+    int best = 1;
+    double best_cost = 1e300;
+    for (int zs = 1; zs <= 32 && zs <= nzi; zs++) {
+        const long long ctas = (long long)ty * tx * zs;
+        const long long waves = (ctas + slots - 1) / slots;
+        const int chunk = (nzi + zs - 1) / zs;
+        const double cost = (double)waves * (chunk + 2.0 * R * 0.5);
+        if (cost < best_cost * 0.999) {
+            best_cost = cost;
+            best = zs;
+        }
+    }
+    return (nzi + best - 1) / best;
+}
+
 template <int R, bool VD>
 size_t smem_bytes() {
     return (size_t)(VD ? 2 : 1) * kStages * Tile<R>::STRIDE * 4 + 128;
@@ -361,25 +628,10 @@ void launch_r(float* un, const float* uc, const float* up, const float* vel, con
     const int ty = (int)((L.ny - 2 * R + 31) / 32);
     const int tx = (int)((L.nx - 2 * R + TL::TX - 1) / TL::TX);
     const int nzi = (int)(L.nz - 2 * R);
-    // z chunks: fill the machine in whole waves, with the 2R-plane warm-up
-    // of every chunk as the cost of splitting
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stencil3d_tiled<R, VD>, kThreads,
                                                   smem);
-    const long long slots = (long long)std::max(per_sm, 1) * device_info().sms;
-    int best = 1;
-    double best_cost = 1e300;
-    for (int zs = 1; zs <= 32 && zs <= nzi; zs++) {
-        const long long ctas = (long long)ty * tx * zs;
-        const long long waves = (ctas + slots - 1) / slots;
-        const int chunk = (nzi + zs - 1) / zs;
-        const double cost = (double)waves * (chunk + 2.0 * R * 0.5);
-        if (cost < best_cost * 0.999) {
-            best_cost = cost;
-            best = zs;
-        }
-    }
-    const int chunk = (nzi + best - 1) / best;
+    const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
     ZeroBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
@@ -431,7 +683,48 @@ __global__ void zero_box_verify(const float* __restrict__ damp, Layout L, int* b
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(box + 6, 1);
 }
 
+
+template <int R, bool VD>
+size_t vec_smem_bytes() {
+    return (size_t)(VD ? 2 : 1) * kStages * VecTile<R>::STRIDE * 4 + 128;
+}
+
+template <int R, bool VD, int MINB>
+void launch_vec(float* un, const float* uc, const float* up, const float* vel, const float* den,
+                const float* damp, const Layout& L, const Weights<float>& W, float dt, float dt2,
+                const TiledContext& ctx, cudaStream_t st) {
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t smem = vec_smem_bytes<R, VD>();
+    if (!configured[dev & 63]) {
+        cudaFuncSetAttribute(stencil3d_vec4<R, VD, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        configured[dev & 63] = true;
+    }
+    const int ty = (int)((L.ny - 2 * R + 127) / 128);
+    const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
+    const int nzi = (int)(L.nz - 2 * R);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stencil3d_vec4<R, VD, MINB>, kThreads,
+                                                  smem);
+    const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
+    const int zsplit = (nzi + chunk - 1) / chunk;
+    const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
+    ZeroBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
+               ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
+    dim3 grid(ty, tx, zsplit);
+    stencil3d_vec4<R, VD, MINB><<<grid, kThreads, smem, st>>>(
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_u_vec),
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_vec), un, uc, up, vel, den, damp, L,
+        W, dt, dt2, (int)cur_slot, chunk, zb, ctx.err);
+}
+
 }  // namespace
+
+static int g_policy = SIMWAVE_POLICY_AUTO;
+int kernel_policy() { return g_policy; }
+void set_kernel_policy(int p) { g_policy = p; }
 
 void find_zero_box(const float* damp, const Layout& L, int* box, cudaStream_t st) {
     cudaMemsetAsync(box, 0, 7 * sizeof(int), st);
@@ -464,6 +757,19 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
     }
     std::memcpy(ctx.map_u, &mu, sizeof(mu));
     std::memcpy(ctx.map_rho, &mr, sizeof(mr));
+    // float4 kernel: orders up to 8, 16-byte aligned rows and arrays
+    ctx.vec = false;
+    if (r <= 4 && (L.lead + r) % 4 == 0) {
+        const int vw = 128 + 2 * round4(r), vh = kWarps + 2 * r;
+        CUtensorMap vu, vr;
+        if (encode_map(&vu, u_base, L, nslots, slot_stride, vw, vh) &&
+            (!vd || encode_map(&vr, den, L, 1, L.nz * L.plane, vw, vh))) {
+            if (!vd) vr = vu;
+            std::memcpy(ctx.map_u_vec, &vu, sizeof(vu));
+            std::memcpy(ctx.map_rho_vec, &vr, sizeof(vr));
+            ctx.vec = true;
+        }
+    }
     ctx.u_base = u_base;
     ctx.slot_stride = slot_stride;
     ctx.ok = true;
@@ -473,6 +779,24 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
 void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, const float* up,
                   const float* vel, const float* den, const float* damp, const Layout& L,
                   const Weights<float>& W, float dt, float dt2, cudaStream_t st) {
+    const int policy = kernel_policy();
+    if (ctx.vec && L.r <= 4 && policy != SIMWAVE_POLICY_SCALAR_TILED &&
+        (reinterpret_cast<uintptr_t>(vel) | reinterpret_cast<uintptr_t>(damp) |
+         reinterpret_cast<uintptr_t>(un) | reinterpret_cast<uintptr_t>(up) |
+         reinterpret_cast<uintptr_t>(uc)) % 16 == 0) {
+        // one CTA per SM without a register cap, or two with a 128 cap
+        const bool one = policy == SIMWAVE_POLICY_VEC_1CTA ||
+                         (policy == SIMWAVE_POLICY_AUTO && vd && L.r >= 3);
+#define SW_VEC(RR)                                                                           \
+    case RR:                                                                                 \
+        if (vd && one) launch_vec<RR, true, 1>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+        else if (vd) launch_vec<RR, true, 2>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st);   \
+        else if (one) launch_vec<RR, false, 1>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+        else launch_vec<RR, false, 2>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st);          \
+        return;
+        switch (L.r) { SW_VEC(1) SW_VEC(2) SW_VEC(3) SW_VEC(4) }
+#undef SW_VEC
+    }
 #define SW_CASE(RR)                                                                    \
     case RR:                                                                           \
         if (vd) launch_r<RR, true>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \

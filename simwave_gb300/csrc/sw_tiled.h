@@ -10,8 +10,11 @@ namespace sw {
 // error word that bounded waits set on expiry.
 struct TiledContext {
     bool ok = false;
-    alignas(64) unsigned char map_u[128];
+    alignas(64) unsigned char map_u[128];      // boxes of the scalar kernel
     alignas(64) unsigned char map_rho[128];
+    alignas(64) unsigned char map_u_vec[128];  // boxes of the float4 kernel
+    alignas(64) unsigned char map_rho_vec[128];
+    bool vec = false;                          // float4 kernel usable
     const float* u_base = nullptr;
     long long slot_stride = 0;
     int zero_box[6] = {0, 0, 0, 0, 0, 0};  // z0, z1, x0, x1, y0, y1 (empty)
@@ -31,6 +34,9 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc,
 // Largest box around the grid centre (interior indices) where `damp` is zero,
 // found and verified on the device; writes {z0, z1, x0, x1, y0, y1} into the
 // device array `box` (7 ints: the 6 bounds and a verification word).
+int kernel_policy();
+void set_kernel_policy(int policy);
+
 void find_zero_box(const float* damp, const Layout& L, int* box, cudaStream_t st);
 
 }  // namespace sw

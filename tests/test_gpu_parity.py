@@ -160,20 +160,29 @@ def test_repeated_calls_are_deterministic():
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
-@pytest.mark.parametrize("order", [2, 4, 8, 10, 16, 20])
+POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3}
+
+
+@pytest.mark.parametrize("policy", list(POLICIES))
+@pytest.mark.parametrize("order", [2, 4, 6, 8, 10, 16, 20])
 @pytest.mark.parametrize("vd", [False, True])
-def test_tiled_and_generic_kernels_agree(order, vd):
-    """The tiled 3D kernel against the one-thread-per-point kernel and the
-    checker, on a shape that leaves partial tiles in x and y."""
+def test_tiled_and_generic_kernels_agree(order, vd, policy):
+    """Each tiled 3D kernel variant against the one-thread-per-point kernel
+    and the checker, on shapes that leave partial tiles in x and y."""
+    from simwave_gb300.backend import _lib
     from simwave_gb300.device import DeviceProblem
-    import torch
     bc = ("null_neumann", "null_dirichlet", "none", "null_neumann",
           "null_dirichlet", "none")
     kw = random_problem(sw, 3, order, vd, bc, 0, shape=(30, 37, 45) if not vd
                         else (30, 41, 41), tf=0.03, seed=order, nrec=5)
     dp = DeviceProblem(kw)
-    st = dp.run()
-    dp.status()
+    lib = _lib.load()
+    assert lib.simwave_set_kernel_policy(POLICIES[policy]) == 0
+    try:
+        st = dp.run()
+        dp.status()
+    finally:
+        lib.simwave_set_kernel_policy(0)
     assert st["stencil_variant"] == 1, "tiled kernel not selected"
     tiled_u, tiled_rec = dp.u_full_numpy(), dp.shot_record_numpy()
     dp.reset()
