@@ -898,7 +898,7 @@ extern "C" int simwave_device_status(void* stream) {
 }
 
 extern "C" int simwave_set_kernel_policy(int policy) {
-    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_1CTA)
+    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_SMEMQ)
         return SIMWAVE_E_ARGUMENT;
     sw::set_kernel_policy(policy);
     return SIMWAVE_OK;

@@ -121,6 +121,7 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
     float* tiles = reinterpret_cast<float*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));  // [NF][kStages][STRIDE]
     __shared__ __align__(8) unsigned long long bars[kStages];
+    __shared__ int s_abort;
     if (*(volatile int*)err) return;  // an earlier launch already failed
 
     const int lane = threadIdx.x & 31;
@@ -140,6 +141,7 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; s++) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
     }
     __syncthreads();
 
@@ -184,6 +186,21 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
         }
     }
 
+    // per-point operands fetched one plane ahead; u_prev with a plain load:
+    // it may be the slot this kernel writes
+    float nprev[NX], nvel[NX], ndamp[NX];
+    auto fetch = [&](int zz) {
+        const long long p = (long long)zz * L.plane;
+        const bool zin = zz >= zb.z0 && zz < zb.z1 && y >= zb.y0 && y < zb.y1;
+#pragma unroll
+        for (int i = 0; i < NX; i++) {
+            nprev[i] = xok[i] ? up[p + off[i]] : 0.f;
+            nvel[i] = xok[i] ? __ldg(vel + p + off[i]) : 0.f;
+            const bool inbox = zin && x0 + i >= zb.x0 && x0 + i < zb.x1;
+            ndamp[i] = (xok[i] && !inbox) ? __ldg(damp + p + off[i]) : 0.f;
+        }
+    };
+    fetch(zbeg);
     int aborted_at = -1;
     for (int z = zbeg; z < zend; z++) {
         const int it = z - zbeg;
@@ -201,24 +218,20 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
                 if (VD) hr[i] = xok[i] ? __ldg(den + pz + off[i]) : 0.f;
             }
         }
-        // per-point operands of this plane
+        // per-point operands of this plane (fetched one plane ahead)
         const long long pz = (long long)z * L.plane;
         float vprev[NX], vvel[NX], vdamp[NX];
-        const bool zin = z >= zb.z0 && z < zb.z1 && y >= zb.y0 && y < zb.y1;
 #pragma unroll
         for (int i = 0; i < NX; i++) {
-            // plain load: u_prev may be the slot this kernel writes
-            vprev[i] = xok[i] ? up[pz + off[i]] : 0.f;
-            vvel[i] = xok[i] ? __ldg(vel + pz + off[i]) : 0.f;
-            const bool inbox = zin && x0 + i >= zb.x0 && x0 + i < zb.x1;
-            vdamp[i] = (xok[i] && !inbox) ? __ldg(damp + pz + off[i]) : 0.f;
+            vprev[i] = nprev[i];
+            vvel[i] = nvel[i];
+            vdamp[i] = ndamp[i];
         }
+        if (z + 1 < zend) fetch(z + 1);
 
         const bool ok = mbar_wait(&bars[stage], (unsigned)((it / kStages) & 1));
-        if (__syncthreads_or(!ok)) {
-            aborted_at = it;
-            break;
-        }
+        if (!ok) s_abort = 1;
+        if (ok) {
         const float* tu = tiles + stage * TL::STRIDE;
         const float* tr = tiles + (kStages + stage) * TL::STRIDE;
         const int cy = lane + HY;  // tile column of this lane
@@ -269,8 +282,13 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
             const float unew = fmaf(dt2 * v2, lap, num) * rden;
             if (xok[i]) un[pz + off[i]] = unew;
         }
+        }  // ok
 
-        __syncthreads();  // everyone is done with this stage's tiles
+        __syncthreads();  // the stage is free again; abort is uniform here
+        if (s_abort) {
+            aborted_at = it;
+            break;
+        }
         if (threadIdx.x == 0 && z + kStages < zend) {
             issue(z + kStages, stage);
             issued++;
@@ -339,7 +357,9 @@ struct VecTile {
     static constexpr int NC = (2 * HY) / 4 + 1;  // float4 chunks of a y window
 };
 
-template <int R, bool VD, int MINB>
+// QS: keep the density z-queue in shared memory (a per-thread circular
+// buffer of 2R+1 float4, read only by its owner) instead of registers.
+template <int R, bool VD, int MINB, bool QS>
 __global__ void __launch_bounds__(kThreads, MINB)
 stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
                const __grid_constant__ CUtensorMap map_rho, float* un,
@@ -354,6 +374,7 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
     float* tiles = reinterpret_cast<float*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     __shared__ __align__(8) unsigned long long bars[kStages];
+    __shared__ int s_abort;
     if (*(volatile int*)err) return;
 
     const int lane = threadIdx.x & 31;
@@ -374,6 +395,7 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; s++) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
     }
     __syncthreads();
     auto issue = [&](int plane, int stage) {
@@ -388,14 +410,20 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
     if (threadIdx.x == 0)
         for (; issued < kStages && zbeg + issued < zend; issued++) issue(zbeg + issued, issued);
 
-    float4 qu[2 * R + 1];
-    float4 qr[VD ? 2 * R + 1 : 1];
+    constexpr int QN = 2 * R + 1;
+    constexpr bool RQ = VD && !QS;  // density queue in registers
+    float4 qu[QN];
+    float4 qr[RQ ? QN : 1];
+    // shared density queue after the TMA stages: [QN][kThreads] float4
+    float4* sq = reinterpret_cast<float4*>(tiles + NF * kStages * VT::STRIDE) + threadIdx.x;
 #pragma unroll
     for (int j = 0; j < 2 * R; j++) {
         const long long pz = (long long)(zbeg - R + j) * L.plane + off;
         qu[j] = ld4(uc + pz, any);
-        if (VD) qr[j] = ld4(den + pz, any);
+        if (RQ) qr[j] = ld4(den + pz, any);
+        if (VD && QS) sq[j * kThreads] = ld4(den + pz, any);
     }
+    int qbase = 0;  // shared queue slot of plane z - R
     float4 hu, hr = f4(0.f);
     {
         const long long pz = (long long)(zbeg + R) * L.plane + off;
@@ -403,43 +431,59 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
         if (VD) hr = ld4(den + pz, any);
     }
 
+    // per-point operands of plane z, fetched one plane ahead; u_prev with a
+    // plain load: it may be the slot this kernel writes (each point reads its
+    // own previous value before writing it)
+    const bool xybox = x >= zb.x0 && x < zb.x1 && y0 >= zb.y0 && y0 + 3 < zb.y1;
+    auto fetch = [&](int zz, float4& pr, float4& ve, float4& da) {
+        const long long p = (long long)zz * L.plane + off;
+        pr = any ? *reinterpret_cast<const float4*>(up + p) : f4(0.f);
+        ve = ld4(vel + p, any);
+        da = ld4(damp + p, any && !(xybox && zz >= zb.z0 && zz < zb.z1));
+    };
+    float4 nprev, nvel, ndamp;
+    fetch(zbeg, nprev, nvel, ndamp);
+
     const float c20 = Wt.c2[0];
     int aborted_at = -1;
     for (int z = zbeg; z < zend; z++) {
         const int it = z - zbeg;
         const int stage = it % kStages;
         qu[2 * R] = hu;
-        if (VD) qr[2 * R] = hr;
+        if (RQ) qr[2 * R] = hr;
+        if (VD && QS) sq[((qbase + 2 * R) % QN) * kThreads] = hr;
+        const float4 vprev = nprev, vvel = nvel, vdamp = ndamp;
         if (z + 1 < zend) {
-            const long long pz = (long long)(z + 1 + R) * L.plane + off;
-            hu = ld4(uc + pz, any);
-            if (VD) hr = ld4(den + pz, any);
+            const long long ph = (long long)(z + 1 + R) * L.plane + off;
+            hu = ld4(uc + ph, any);
+            if (VD) hr = ld4(den + ph, any);
+            fetch(z + 1, nprev, nvel, ndamp);
         }
         const long long pz = (long long)z * L.plane + off;
-        // u_prev with a plain load: it may be the slot this kernel writes
-        const float4 vprev = any ? *reinterpret_cast<const float4*>(up + pz) : f4(0.f);
-        const float4 vvel = ld4(vel + pz, any);
-        const bool inbox = z >= zb.z0 && z < zb.z1 && x >= zb.x0 && x < zb.x1 &&
-                           y0 >= zb.y0 && y0 + 3 < zb.y1;
-        const float4 vdamp = ld4(damp + pz, any && !inbox);
 
         // z axis: register queues
         const float4 u0 = qu[R];
         float4 sdz = mul4(c20, u0), fuz = f4(0.f), frz = f4(0.f);
+        float4 rho0 = f4(1.f);
 #pragma unroll
         for (int k = 1; k <= R; k++) {
             sdz = fma4(Wt.c2[k], add4(qu[R + k], qu[R - k]), sdz);
             if (VD) {
                 fuz = fma4(Wt.c1[k], sub4(qu[R + k], qu[R - k]), fuz);
-                frz = fma4(Wt.c1[k], sub4(qr[R + k], qr[R - k]), frz);
+                if (RQ) {
+                    frz = fma4(Wt.c1[k], sub4(qr[R + k], qr[R - k]), frz);
+                } else {
+                    const float4 pa = sq[((qbase + R + k) % QN) * kThreads];
+                    const float4 pb = sq[((qbase + R - k) % QN) * kThreads];
+                    frz = fma4(Wt.c1[k], sub4(pa, pb), frz);
+                }
             }
         }
+        if (VD) rho0 = RQ ? qr[R] : sq[((qbase + R) % QN) * kThreads];
 
         const bool ok = mbar_wait(&bars[stage], (unsigned)((it / kStages) & 1));
-        if (__syncthreads_or(!ok)) {
-            aborted_at = it;
-            break;
-        }
+        if (!ok) s_abort = 1;
+        if (ok) {
         const float* tu = tiles + stage * VT::STRIDE + (warp + R) * TW + 4 * lane;
         const float* tr = tiles + (kStages + stage) * VT::STRIDE + (warp + R) * TW + 4 * lane;
 
@@ -504,7 +548,7 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
                 float cross = comp(fuy, v) * comp(fry, v) * Wt.s1[2] +
                               comp(fux, v) * comp(frx, v) * Wt.s1[1];
                 cross = fmaf(comp(fuz, v) * comp(frz, v), Wt.s1[0], cross);
-                lap -= __fdividef(cross, comp(qr[R], v));
+                lap -= __fdividef(cross, comp(rho0, v));
             }
             const float vv = comp(vvel, v);
             const float v2 = vv * vv;
@@ -520,8 +564,13 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
             for (int v = 0; v < 4; v++)
                 if (y0 + v < ylim) un[pz + v] = comp(out, v);
         }
+        }  // ok
 
-        __syncthreads();
+        __syncthreads();  // the stage is free again; abort is uniform here
+        if (s_abort) {
+            aborted_at = it;
+            break;
+        }
         if (threadIdx.x == 0 && z + kStages < zend) {
             issue(z + kStages, stage);
             issued++;
@@ -529,8 +578,9 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
 #pragma unroll
         for (int j = 0; j < 2 * R; j++) {
             qu[j] = qu[j + 1];
-            if (VD) qr[j] = qr[j + 1];
+            if (RQ) qr[j] = qr[j + 1];
         }
+        qbase = qbase + 1 == QN ? 0 : qbase + 1;
     }
     if (aborted_at >= 0 && threadIdx.x == 0) {
         atomicExch(err, SIMWAVE_E_TIMEOUT);
@@ -684,21 +734,22 @@ __global__ void zero_box_verify(const float* __restrict__ damp, Layout L, int* b
 }
 
 
-template <int R, bool VD>
+template <int R, bool VD, bool QS>
 size_t vec_smem_bytes() {
-    return (size_t)(VD ? 2 : 1) * kStages * VecTile<R>::STRIDE * 4 + 128;
+    const size_t queue = (VD && QS) ? (size_t)(2 * R + 1) * kThreads * 16 : 0;
+    return (size_t)(VD ? 2 : 1) * kStages * VecTile<R>::STRIDE * 4 + queue + 128;
 }
 
-template <int R, bool VD, int MINB>
+template <int R, bool VD, int MINB, bool QS>
 void launch_vec(float* un, const float* uc, const float* up, const float* vel, const float* den,
                 const float* damp, const Layout& L, const Weights<float>& W, float dt, float dt2,
                 const TiledContext& ctx, cudaStream_t st) {
     static bool configured[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
-    const size_t smem = vec_smem_bytes<R, VD>();
+    const size_t smem = vec_smem_bytes<R, VD, QS>();
     if (!configured[dev & 63]) {
-        cudaFuncSetAttribute(stencil3d_vec4<R, VD, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(stencil3d_vec4<R, VD, MINB, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         configured[dev & 63] = true;
     }
@@ -706,7 +757,7 @@ void launch_vec(float* un, const float* uc, const float* up, const float* vel, c
     const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
     const int nzi = (int)(L.nz - 2 * R);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stencil3d_vec4<R, VD, MINB>, kThreads,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stencil3d_vec4<R, VD, MINB, QS>, kThreads,
                                                   smem);
     const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
     const int zsplit = (nzi + chunk - 1) / chunk;
@@ -714,7 +765,7 @@ void launch_vec(float* un, const float* uc, const float* up, const float* vel, c
     ZeroBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
                ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
     dim3 grid(ty, tx, zsplit);
-    stencil3d_vec4<R, VD, MINB><<<grid, kThreads, smem, st>>>(
+    stencil3d_vec4<R, VD, MINB, QS><<<grid, kThreads, smem, st>>>(
         *reinterpret_cast<const CUtensorMap*>(ctx.map_u_vec),
         *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_vec), un, uc, up, vel, den, damp, L,
         W, dt, dt2, (int)cur_slot, chunk, zb, ctx.err);
@@ -784,15 +835,18 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, 
         (reinterpret_cast<uintptr_t>(vel) | reinterpret_cast<uintptr_t>(damp) |
          reinterpret_cast<uintptr_t>(un) | reinterpret_cast<uintptr_t>(up) |
          reinterpret_cast<uintptr_t>(uc)) % 16 == 0) {
-        // one CTA per SM without a register cap, or two with a 128 cap
-        const bool one = policy == SIMWAVE_POLICY_VEC_1CTA ||
-                         (policy == SIMWAVE_POLICY_AUTO && vd && L.r >= 3);
-#define SW_VEC(RR)                                                                           \
-    case RR:                                                                                 \
-        if (vd && one) launch_vec<RR, true, 1>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
-        else if (vd) launch_vec<RR, true, 2>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st);   \
-        else if (one) launch_vec<RR, false, 1>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
-        else launch_vec<RR, false, 2>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st);          \
+        // one CTA per SM without a register cap, two with a 128 cap, or two
+        // with the density queue in shared memory
+        const bool one = policy == SIMWAVE_POLICY_VEC_1CTA;
+        const bool qs = policy == SIMWAVE_POLICY_VEC_SMEMQ ||
+                        (policy == SIMWAVE_POLICY_AUTO && vd && L.r >= 3);
+#define SW_VEC(RR)                                                                             \
+    case RR:                                                                                   \
+        if (vd && qs) launch_vec<RR, true, 2, true>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+        else if (vd && one) launch_vec<RR, true, 1, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+        else if (vd) launch_vec<RR, true, 2, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+        else if (one) launch_vec<RR, false, 1, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+        else launch_vec<RR, false, 2, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
         return;
         switch (L.r) { SW_VEC(1) SW_VEC(2) SW_VEC(3) SW_VEC(4) }
 #undef SW_VEC

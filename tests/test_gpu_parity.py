@@ -160,7 +160,8 @@ def test_repeated_calls_are_deterministic():
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
-POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3}
+POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3,
+            "vec_smemq": 4}
 
 
 @pytest.mark.parametrize("policy", list(POLICIES))
