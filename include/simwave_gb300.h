@@ -253,6 +253,9 @@ int simwave_forward_device(const simwave_problem *problem, void *stream);
 #define SIMWAVE_POLICY_VEC_1CTA 3       /* float4 along y, 1 CTA per SM */
 #define SIMWAVE_POLICY_VEC_SMEMQ 4      /* float4 along y, density z-queue in
                                            shared memory, 2 CTAs per SM */
+#define SIMWAVE_POLICY_VEC_2CTA_ROT 5   /* float4, register queues rotated by
+                                           unrolling, 2 CTAs per SM */
+#define SIMWAVE_POLICY_VEC_1CTA_ROT 6   /* same, 1 CTA per SM */
 int simwave_set_kernel_policy(int policy);
 
 /* Wait for `stream` and report device-side failures of the forward calls

@@ -230,8 +230,8 @@ static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
     const T dt2 = R.dt * R.dt;
     if constexpr (std::is_same<T, float>::value && DIM == 3) {
         if (tctx.ok) {
-            tiled_launch(tctx, VD, un, uc, up, R.vel, R.den, R.damp, L, R.W,
-                         R.dt, dt2, st);
+            tiled_launch(tctx, VD, un, uc, up, tctx.coefC, R.den, tctx.coefQ, L,
+                         R.W, R.dt, dt2, st);
             *variant = 1;
             SW_LAUNCHED("stencil3d_tiled");
             return;
@@ -264,6 +264,16 @@ static int* device_words() {
     return w;
 }
 
+// Scratch for the per-point coefficients of the tiled kernels (floats).
+static float* coefficient_scratch(size_t count) {
+    static std::mutex m;
+    static std::map<int, Buffer> bufs;
+    int dev = 0;
+    SW_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(m);
+    return (float*)bufs[dev].ensure(count * sizeof(float));
+}
+
 // Tiled-kernel context of one run (float32 3D only).
 template <typename T>
 static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
@@ -273,8 +283,17 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         if (!tiled_prepare(ctx, R.L, R.vd, R.u, (long long)R.nslots,
                            (long long)R.L.slot, R.den))
             return ctx;
+        // per-point coefficients C, Q in library scratch (grow-only, per device)
+        float* cq = coefficient_scratch((size_t)R.L.slot * 2);
+        float* C = cq;
+        float* Q = cq + R.L.slot;
+        const long long n = R.L.dim == 3 ? R.L.nz * R.L.plane : R.L.nz * R.L.pitch;
+        form_coefficients(R.vel, R.damp, C, Q, n, (float)R.dt, st);
+        SW_LAUNCHED("form_coefficients");
+        ctx.coefC = C;
+        ctx.coefQ = Q;
         int* words = device_words();
-        find_zero_box(R.damp, R.L, words, st);
+        find_zero_box(Q, R.L, words, st);
         SW_LAUNCHED("find_zero_box");
         int box[7];
         SW_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
@@ -898,7 +917,7 @@ extern "C" int simwave_device_status(void* stream) {
 }
 
 extern "C" int simwave_set_kernel_policy(int policy) {
-    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_SMEMQ)
+    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_1CTA_ROT)
         return SIMWAVE_E_ARGUMENT;
     sw::set_kernel_policy(policy);
     return SIMWAVE_OK;

@@ -54,6 +54,9 @@ struct Tile {
 
 // ---- PTX helpers -----------------------------------------------------------
 
+// The kernels' only shared memory: one dynamic region per CTA.
+extern __shared__ __align__(128) float4 sw_dyn_smem[];
+
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
 }
@@ -98,6 +101,39 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map,
         : "memory");
 }
 
+// ---- per-point coefficients --------------------------------------------------
+//
+// The tiled kernels read two time-invariant per-point coefficients instead of
+// velocity and damping, formed once per run exactly as the reference forms
+// them every step (constant_density/2d/wave.c:170-178):
+//   Q = damp * dt / (2 * slowness),  slowness = 1 / v^2
+//   C = (dt^2 / slowness) / (1 + Q)
+// so that u_next = 2/D u_cur - N/D u_prev + C L(u_cur), D = 1 + Q, N = 1 - Q.
+// Q is zero wherever the damping mask is, so its loads are skipped there.
+
+__global__ void form_coefficients(const float* __restrict__ vel,
+                                  const float* __restrict__ damp, float* __restrict__ C,
+                                  float* __restrict__ Q, long long n, float dt) {
+    const float dt2 = dt * dt;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float v = vel[i];
+        const float slowness = __frcp_rn(v * v);
+        const float q = __fdiv_rn(damp[i] * dt, 2.f * slowness);
+        const float den = 1.f + q;
+        C[i] = __fdiv_rn(__fdiv_rn(dt2, slowness), den);
+        Q[i] = q;
+    }
+}
+
+// u_next from the spatial operator, C, Q, u_cur and u_prev.
+__device__ __forceinline__ float leapfrog_cq(float lap, float c, float q, float ucur,
+                                             float uprev) {
+    const float a = fmaf(-(1.f - q), uprev, 2.f * ucur);
+    const float b = q == 0.f ? a : a * __fdividef(1.f, 1.f + q);
+    return fmaf(lap, c, b);
+}
+
 // ---- the kernel ------------------------------------------------------------
 
 struct ZeroBox {  // interior box where the damping mask is zero
@@ -116,13 +152,18 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
     using TL = Tile<R>;
     constexpr int NX = TL::NX, TX = TL::TX, HY = TL::HY, TW = TL::W;
     constexpr int NF = VD ? 2 : 1;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    // TMA destinations 128-byte aligned whatever the dynamic base alignment
-    float* tiles = reinterpret_cast<float*>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));  // [NF][kStages][STRIDE]
-    __shared__ __align__(8) unsigned long long bars[kStages];
-    __shared__ int s_abort;
+    // dynamic shared memory only (no static shared data), so the region
+    // starts at the base of the CTA's shared window: 128-byte aligned TMA
+    // destinations, then the mbarriers and the abort flag
+    float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [NF][kStages][STRIDE]
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(tiles + NF * kStages * TL::STRIDE);
+    int& s_abort = *reinterpret_cast<int*>(bars + kStages);
     if (*(volatile int*)err) return;  // an earlier launch already failed
+    if (smem_addr(tiles) & 127) {    // layout assumption broken: refuse
+        if (threadIdx.x == 0) atomicExch(err, SIMWAVE_E_ARGUMENT);
+        return;
+    }
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -275,11 +316,7 @@ stencil3d_tiled(const __grid_constant__ CUtensorMap map_u,
                 cross = fmaf(gz * rz, Wt.s1[0], cross);
                 lap -= __fdividef(cross, qr[i][R]);
             }
-            const float v2 = vvel[i] * vvel[i];
-            const float q = vdamp[i] * dt * v2 * 0.5f;
-            const float rden = __frcp_rn(1.f + q);
-            const float num = fmaf(-(1.f - q), vprev[i], 2.f * u0);
-            const float unew = fmaf(dt2 * v2, lap, num) * rden;
+            const float unew = leapfrog_cq(lap, vvel[i], vdamp[i], u0, vprev[i]);
             if (xok[i]) un[pz + off[i]] = unew;
         }
         }  // ok
@@ -359,23 +396,34 @@ struct VecTile {
 
 // QS: keep the density z-queue in shared memory (a per-thread circular
 // buffer of 2R+1 float4, read only by its owner) instead of registers.
-template <int R, bool VD, int MINB, bool QS>
+// ROT: unroll the plane loop by the queue length 2R+1 so that queue slots are
+// compile-time constants (no register moves, no index arithmetic).
+// Queue slot of plane p: (p - zbeg + R) mod (2R+1).
+template <int R, bool VD, int MINB, bool QS, bool ROT>
 __global__ void __launch_bounds__(kThreads, MINB)
 stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
                const __grid_constant__ CUtensorMap map_rho, float* un,
                const float* __restrict__ uc, const float* up,
-               const float* __restrict__ vel, const float* __restrict__ den,
-               const float* __restrict__ damp, Layout L, Weights<float> Wt, float dt,
-               float dt2, int slot_cur, int zchunk, ZeroBox zb, int* __restrict__ err) {
+               const float* __restrict__ coefC, const float* __restrict__ den,
+               const float* __restrict__ coefQ, Layout L, Weights<float> Wt,
+               int slot_cur, int zchunk, ZeroBox zb, int* __restrict__ err) {
     using VT = VecTile<R>;
     constexpr int HY = VT::HY, TW = VT::TW, NC = VT::NC;
     constexpr int NF = VD ? 2 : 1;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* tiles = reinterpret_cast<float*>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    __shared__ __align__(8) unsigned long long bars[kStages];
-    __shared__ int s_abort;
+    constexpr int QN = 2 * R + 1;
+    constexpr bool RQ = VD && !QS;  // density queue in registers
+    // dynamic shared memory only: TMA tiles (128-byte aligned), the shared
+    // density queue, then the mbarriers and the abort flag
+    float* tiles = reinterpret_cast<float*>(sw_dyn_smem);
+    float4* sq_base = reinterpret_cast<float4*>(tiles + NF * kStages * VT::STRIDE);
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(sq_base + (VD && QS ? QN * kThreads : 0));
+    int& s_abort = *reinterpret_cast<int*>(bars + kStages);
     if (*(volatile int*)err) return;
+    if (smem_addr(tiles) & 127) {
+        if (threadIdx.x == 0) atomicExch(err, SIMWAVE_E_ARGUMENT);
+        return;
+    }
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -410,177 +458,183 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
     if (threadIdx.x == 0)
         for (; issued < kStages && zbeg + issued < zend; issued++) issue(zbeg + issued, issued);
 
-    constexpr int QN = 2 * R + 1;
-    constexpr bool RQ = VD && !QS;  // density queue in registers
+    // queues hold planes z-R .. z+R; slot of plane p = (p - zbeg + R) mod QN
     float4 qu[QN];
     float4 qr[RQ ? QN : 1];
-    // shared density queue after the TMA stages: [QN][kThreads] float4
-    float4* sq = reinterpret_cast<float4*>(tiles + NF * kStages * VT::STRIDE) + threadIdx.x;
+    float4* sq = sq_base + threadIdx.x;
 #pragma unroll
-    for (int j = 0; j < 2 * R; j++) {
+    for (int j = 0; j < QN; j++) {
         const long long pz = (long long)(zbeg - R + j) * L.plane + off;
         qu[j] = ld4(uc + pz, any);
         if (RQ) qr[j] = ld4(den + pz, any);
         if (VD && QS) sq[j * kThreads] = ld4(den + pz, any);
     }
-    int qbase = 0;  // shared queue slot of plane z - R
-    float4 hu, hr = f4(0.f);
-    {
-        const long long pz = (long long)(zbeg + R) * L.plane + off;
-        hu = ld4(uc + pz, any);
-        if (VD) hr = ld4(den + pz, any);
-    }
-
-    // per-point operands of plane z, fetched one plane ahead; u_prev with a
-    // plain load: it may be the slot this kernel writes (each point reads its
-    // own previous value before writing it)
+    // per-point operands of the next plane; u_prev with a plain load: it may
+    // be the slot this kernel writes (each point reads its own previous value
+    // before writing it)
     const bool xybox = x >= zb.x0 && x < zb.x1 && y0 >= zb.y0 && y0 + 3 < zb.y1;
-    auto fetch = [&](int zz, float4& pr, float4& ve, float4& da) {
+    float4 nprev, ncoef, nq;
+    auto fetch = [&](int zz) {
         const long long p = (long long)zz * L.plane + off;
-        pr = any ? *reinterpret_cast<const float4*>(up + p) : f4(0.f);
-        ve = ld4(vel + p, any);
-        da = ld4(damp + p, any && !(xybox && zz >= zb.z0 && zz < zb.z1));
+        nprev = any ? *reinterpret_cast<const float4*>(up + p) : f4(0.f);
+        ncoef = ld4(coefC + p, any);
+        nq = ld4(coefQ + p, any && !(xybox && zz >= zb.z0 && zz < zb.z1));
     };
-    float4 nprev, nvel, ndamp;
-    fetch(zbeg, nprev, nvel, ndamp);
-
+    fetch(zbeg);
     const float c20 = Wt.c2[0];
     int aborted_at = -1;
-    for (int z = zbeg; z < zend; z++) {
+    static_assert(ROT || !QS, "the shared density queue needs the unrolled plane loop");
+
+    // one plane; J = (z - zbeg) mod QN when known at compile time (ROT)
+    auto plane_step = [&](const int z, const int J) -> bool {
         const int it = z - zbeg;
         const int stage = it % kStages;
-        qu[2 * R] = hu;
-        if (RQ) qr[2 * R] = hr;
-        if (VD && QS) sq[((qbase + 2 * R) % QN) * kThreads] = hr;
-        const float4 vprev = nprev, vvel = nvel, vdamp = ndamp;
-        if (z + 1 < zend) {
+        auto slot = [&](int d) { return (J + R + d) % QN; };  // plane z + d
+        const float4 vprev = nprev, vcoef = ncoef, vq = nq;
+        float4 hu = f4(0.f), hr = f4(0.f);
+        const bool more = z + 1 < zend;
+        if (more) {
             const long long ph = (long long)(z + 1 + R) * L.plane + off;
             hu = ld4(uc + ph, any);
             if (VD) hr = ld4(den + ph, any);
-            fetch(z + 1, nprev, nvel, ndamp);
+            fetch(z + 1);
         }
         const long long pz = (long long)z * L.plane + off;
 
-        // z axis: register queues
-        const float4 u0 = qu[R];
+        // z axis: queues
+        const float4 u0 = qu[slot(0)];
         float4 sdz = mul4(c20, u0), fuz = f4(0.f), frz = f4(0.f);
-        float4 rho0 = f4(1.f);
 #pragma unroll
         for (int k = 1; k <= R; k++) {
-            sdz = fma4(Wt.c2[k], add4(qu[R + k], qu[R - k]), sdz);
+            const float4 a = qu[slot(k)], b = qu[slot(-k)];
+            sdz = fma4(Wt.c2[k], add4(a, b), sdz);
             if (VD) {
-                fuz = fma4(Wt.c1[k], sub4(qu[R + k], qu[R - k]), fuz);
-                if (RQ) {
-                    frz = fma4(Wt.c1[k], sub4(qr[R + k], qr[R - k]), frz);
-                } else {
-                    const float4 pa = sq[((qbase + R + k) % QN) * kThreads];
-                    const float4 pb = sq[((qbase + R - k) % QN) * kThreads];
-                    frz = fma4(Wt.c1[k], sub4(pa, pb), frz);
-                }
+                fuz = fma4(Wt.c1[k], sub4(a, b), fuz);
+                const float4 pa = RQ ? qr[slot(k)] : sq[slot(k) * kThreads];
+                const float4 pb = RQ ? qr[slot(-k)] : sq[slot(-k) * kThreads];
+                frz = fma4(Wt.c1[k], sub4(pa, pb), frz);
             }
         }
-        if (VD) rho0 = RQ ? qr[R] : sq[((qbase + R) % QN) * kThreads];
+        float4 rho0 = f4(1.f);
+        if (VD) rho0 = RQ ? qr[slot(0)] : sq[slot(0) * kThreads];
 
         const bool ok = mbar_wait(&bars[stage], (unsigned)((it / kStages) & 1));
         if (!ok) s_abort = 1;
         if (ok) {
-        const float* tu = tiles + stage * VT::STRIDE + (warp + R) * TW + 4 * lane;
-        const float* tr = tiles + (kStages + stage) * VT::STRIDE + (warp + R) * TW + 4 * lane;
-
-        // x axis: rows x +- k of the tile, this thread's 4 columns
-        float4 sdx = mul4(c20, u0), fux = f4(0.f), frx = f4(0.f);
-#pragma unroll
-        for (int k = 1; k <= R; k++) {
-            const float4 a = *reinterpret_cast<const float4*>(tu + k * TW + HY);
-            const float4 b = *reinterpret_cast<const float4*>(tu - k * TW + HY);
-            sdx = fma4(Wt.c2[k], add4(a, b), sdx);
-            if (VD) {
-                fux = fma4(Wt.c1[k], sub4(a, b), fux);
-                const float4 ra = *reinterpret_cast<const float4*>(tr + k * TW + HY);
-                const float4 rb = *reinterpret_cast<const float4*>(tr - k * TW + HY);
-                frx = fma4(Wt.c1[k], sub4(ra, rb), frx);
-            }
-        }
-
-        // y axis: window of 4 + 2*HY values of this thread's row
-        float wu[4 * NC];
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const float4 t = *reinterpret_cast<const float4*>(tu + 4 * c);
-            wu[4 * c] = t.x; wu[4 * c + 1] = t.y; wu[4 * c + 2] = t.z; wu[4 * c + 3] = t.w;
-        }
-        float4 sdy = mul4(c20, u0), fuy = f4(0.f), fry = f4(0.f);
-#pragma unroll
-        for (int v = 0; v < 4; v++) {
-            float s = comp(sdy, v), g = 0.f;
+            const float* tu = tiles + stage * VT::STRIDE + (warp + R) * TW + 4 * lane;
+            const float* tr = tiles + (kStages + stage) * VT::STRIDE + (warp + R) * TW + 4 * lane;
+            // x axis: rows x +- k of the tile, this thread's 4 columns
+            float4 sdx = mul4(c20, u0), fux = f4(0.f), frx = f4(0.f);
 #pragma unroll
             for (int k = 1; k <= R; k++) {
-                s = fmaf(Wt.c2[k], wu[HY + v + k] + wu[HY + v - k], s);
-                if (VD) g = fmaf(Wt.c1[k], wu[HY + v + k] - wu[HY + v - k], g);
+                const float4 a = *reinterpret_cast<const float4*>(tu + k * TW + HY);
+                const float4 b = *reinterpret_cast<const float4*>(tu - k * TW + HY);
+                sdx = fma4(Wt.c2[k], add4(a, b), sdx);
+                if (VD) {
+                    fux = fma4(Wt.c1[k], sub4(a, b), fux);
+                    const float4 ra = *reinterpret_cast<const float4*>(tr + k * TW + HY);
+                    const float4 rb = *reinterpret_cast<const float4*>(tr - k * TW + HY);
+                    frx = fma4(Wt.c1[k], sub4(ra, rb), frx);
+                }
             }
-            set_comp(sdy, v, s);
-            set_comp(fuy, v, g);
-        }
-        if (VD) {
-            float wr[4 * NC];
+            // y axis: window of 4 + 2*HY values of this thread's row
+            float wu[4 * NC];
 #pragma unroll
             for (int c = 0; c < NC; c++) {
-                const float4 t = *reinterpret_cast<const float4*>(tr + 4 * c);
-                wr[4 * c] = t.x; wr[4 * c + 1] = t.y; wr[4 * c + 2] = t.z; wr[4 * c + 3] = t.w;
+                const float4 t = *reinterpret_cast<const float4*>(tu + 4 * c);
+                wu[4 * c] = t.x; wu[4 * c + 1] = t.y; wu[4 * c + 2] = t.z; wu[4 * c + 3] = t.w;
             }
+            float4 sdy = mul4(c20, u0), fuy = f4(0.f), fry = f4(0.f);
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                float g = 0.f;
+                float sy = comp(sdy, v), g = 0.f;
 #pragma unroll
-                for (int k = 1; k <= R; k++)
-                    g = fmaf(Wt.c1[k], wr[HY + v + k] - wr[HY + v - k], g);
-                set_comp(fry, v, g);
+                for (int k = 1; k <= R; k++) {
+                    sy = fmaf(Wt.c2[k], wu[HY + v + k] + wu[HY + v - k], sy);
+                    if (VD) g = fmaf(Wt.c1[k], wu[HY + v + k] - wu[HY + v - k], g);
+                }
+                set_comp(sdy, v, sy);
+                set_comp(fuy, v, g);
             }
-        }
-
-        // combine (reference order y, x, z) and update
-        float4 out;
-#pragma unroll
-        for (int v = 0; v < 4; v++) {
-            float lap = comp(sdy, v) * Wt.ih2[2] + comp(sdx, v) * Wt.ih2[1];
-            lap = fmaf(comp(sdz, v), Wt.ih2[0], lap);
             if (VD) {
-                float cross = comp(fuy, v) * comp(fry, v) * Wt.s1[2] +
-                              comp(fux, v) * comp(frx, v) * Wt.s1[1];
-                cross = fmaf(comp(fuz, v) * comp(frz, v), Wt.s1[0], cross);
-                lap -= __fdividef(cross, comp(rho0, v));
-            }
-            const float vv = comp(vvel, v);
-            const float v2 = vv * vv;
-            const float q = comp(vdamp, v) * dt * v2 * 0.5f;
-            const float rden = __frcp_rn(1.f + q);
-            const float num = fmaf(-(1.f - q), comp(vprev, v), 2.f * comp(u0, v));
-            set_comp(out, v, fmaf(dt2 * v2, lap, num) * rden);
-        }
-        if (full) {
-            *reinterpret_cast<float4*>(un + pz) = out;
-        } else if (any) {
+                float wr[4 * NC];
 #pragma unroll
-            for (int v = 0; v < 4; v++)
-                if (y0 + v < ylim) un[pz + v] = comp(out, v);
+                for (int c = 0; c < NC; c++) {
+                    const float4 t = *reinterpret_cast<const float4*>(tr + 4 * c);
+                    wr[4 * c] = t.x; wr[4 * c + 1] = t.y; wr[4 * c + 2] = t.z; wr[4 * c + 3] = t.w;
+                }
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    float g = 0.f;
+#pragma unroll
+                    for (int k = 1; k <= R; k++)
+                        g = fmaf(Wt.c1[k], wr[HY + v + k] - wr[HY + v - k], g);
+                    set_comp(fry, v, g);
+                }
+            }
+            // combine (reference order y, x, z) and update
+            float4 out;
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                float lap = comp(sdy, v) * Wt.ih2[2] + comp(sdx, v) * Wt.ih2[1];
+                lap = fmaf(comp(sdz, v), Wt.ih2[0], lap);
+                if (VD) {
+                    float cross = comp(fuy, v) * comp(fry, v) * Wt.s1[2] +
+                                  comp(fux, v) * comp(frx, v) * Wt.s1[1];
+                    cross = fmaf(comp(fuz, v) * comp(frz, v), Wt.s1[0], cross);
+                    lap -= __fdividef(cross, comp(rho0, v));
+                }
+                set_comp(out, v, leapfrog_cq(lap, comp(vcoef, v), comp(vq, v), comp(u0, v),
+                                             comp(vprev, v)));
+            }
+            if (full) {
+                *reinterpret_cast<float4*>(un + pz) = out;
+            } else if (any) {
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    if (y0 + v < ylim) un[pz + v] = comp(out, v);
+            }
         }
-        }  // ok
-
         __syncthreads();  // the stage is free again; abort is uniform here
         if (s_abort) {
             aborted_at = it;
-            break;
+            return false;
         }
         if (threadIdx.x == 0 && z + kStages < zend) {
             issue(z + kStages, stage);
             issued++;
         }
+        // plane z - R leaves the queues; plane z + R + 1 takes its slot
+        if (more) {
+            if (ROT) {
+                qu[slot(-R)] = hu;
+                if (RQ) qr[slot(-R)] = hr;
+            } else {
 #pragma unroll
-        for (int j = 0; j < 2 * R; j++) {
-            qu[j] = qu[j + 1];
-            if (RQ) qr[j] = qr[j + 1];
+                for (int j = 0; j < QN - 1; j++) {
+                    qu[j] = qu[j + 1];
+                    if (RQ) qr[j] = qr[j + 1];
+                }
+                qu[QN - 1] = hu;
+                if (RQ) qr[QN - 1] = hr;
+            }
+            if (VD && QS) sq[slot(-R) * kThreads] = hr;
         }
-        qbase = qbase + 1 == QN ? 0 : qbase + 1;
+        return true;
+    };
+
+    if (ROT) {
+        for (int zb0 = zbeg; zb0 < zend; zb0 += QN) {
+#pragma unroll
+            for (int J = 0; J < QN; J++) {
+                if (zb0 + J >= zend || !plane_step(zb0 + J, J)) break;
+            }
+            if (aborted_at >= 0) break;
+        }
+    } else {
+        // register queues shifted every plane: plane z + d sits in slot R + d
+        for (int z = zbeg; z < zend; z++)
+            if (!plane_step(z, 0)) break;
     }
     if (aborted_at >= 0 && threadIdx.x == 0) {
         atomicExch(err, SIMWAVE_E_TIMEOUT);
@@ -658,7 +712,7 @@ int choose_chunk(int ty, int tx, int nzi, int R, int per_sm) {
 
 template <int R, bool VD>
 size_t smem_bytes() {
-    return (size_t)(VD ? 2 : 1) * kStages * Tile<R>::STRIDE * 4 + 128;
+    return (size_t)(VD ? 2 : 1) * kStages * Tile<R>::STRIDE * 4 + 64;
 }
 
 template <int R, bool VD>
@@ -737,41 +791,65 @@ __global__ void zero_box_verify(const float* __restrict__ damp, Layout L, int* b
 template <int R, bool VD, bool QS>
 size_t vec_smem_bytes() {
     const size_t queue = (VD && QS) ? (size_t)(2 * R + 1) * kThreads * 16 : 0;
-    return (size_t)(VD ? 2 : 1) * kStages * VecTile<R>::STRIDE * 4 + queue + 128;
+    return (size_t)(VD ? 2 : 1) * kStages * VecTile<R>::STRIDE * 4 + queue + 64;
 }
 
-template <int R, bool VD, int MINB, bool QS>
-void launch_vec(float* un, const float* uc, const float* up, const float* vel, const float* den,
-                const float* damp, const Layout& L, const Weights<float>& W, float dt, float dt2,
+template <int R, bool VD, int MINB, bool QS, bool ROT>
+void launch_vec(float* un, const float* uc, const float* up, const float* coefC,
+                const float* den, const float* coefQ, const Layout& L, const Weights<float>& W,
                 const TiledContext& ctx, cudaStream_t st) {
+    auto kernel = stencil3d_vec4<R, VD, MINB, QS, ROT>;
     static bool configured[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     const size_t smem = vec_smem_bytes<R, VD, QS>();
     if (!configured[dev & 63]) {
-        cudaFuncSetAttribute(stencil3d_vec4<R, VD, MINB, QS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[dev & 63] = true;
     }
     const int ty = (int)((L.ny - 2 * R + 127) / 128);
     const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
     const int nzi = (int)(L.nz - 2 * R);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stencil3d_vec4<R, VD, MINB, QS>, kThreads,
-                                                  smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
     const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
     ZeroBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
                ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
     dim3 grid(ty, tx, zsplit);
-    stencil3d_vec4<R, VD, MINB, QS><<<grid, kThreads, smem, st>>>(
+    kernel<<<grid, kThreads, smem, st>>>(
         *reinterpret_cast<const CUtensorMap*>(ctx.map_u_vec),
-        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_vec), un, uc, up, vel, den, damp, L,
-        W, dt, dt2, (int)cur_slot, chunk, zb, ctx.err);
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_vec), un, uc, up, coefC, den, coefQ,
+        L, W, (int)cur_slot, chunk, zb, ctx.err);
 }
 
+template <int R, bool VD>
+void launch_vec_policy(int policy, float* un, const float* uc, const float* up,
+                       const float* coefC, const float* den, const float* coefQ,
+                       const Layout& L, const Weights<float>& W, const TiledContext& ctx,
+                       cudaStream_t st) {
+    if (policy == SIMWAVE_POLICY_AUTO)
+        policy = (VD && R >= 3) ? SIMWAVE_POLICY_VEC_SMEMQ : SIMWAVE_POLICY_VEC_2CTA_ROT;
+    switch (policy) {
+        case SIMWAVE_POLICY_VEC_2CTA:
+            return launch_vec<R, VD, 2, false, false>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+        case SIMWAVE_POLICY_VEC_1CTA:
+            return launch_vec<R, VD, 1, false, false>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+        case SIMWAVE_POLICY_VEC_SMEMQ:
+            return launch_vec<R, VD, 2, VD, true>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+        case SIMWAVE_POLICY_VEC_2CTA_ROT:
+            return launch_vec<R, VD, 2, false, true>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+        default:  // SIMWAVE_POLICY_VEC_1CTA_ROT
+            return launch_vec<R, VD, 1, false, true>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+    }
+}
 }  // namespace
+
+void form_coefficients(const float* vel, const float* damp, float* C, float* Q,
+                       long long n, float dt, cudaStream_t st) {
+    form_coefficients<<<device_info().sms * 8, 256, 0, st>>>(vel, damp, C, Q, n, dt);
+}
 
 static int g_policy = SIMWAVE_POLICY_AUTO;
 int kernel_policy() { return g_policy; }
@@ -835,18 +913,10 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, 
         (reinterpret_cast<uintptr_t>(vel) | reinterpret_cast<uintptr_t>(damp) |
          reinterpret_cast<uintptr_t>(un) | reinterpret_cast<uintptr_t>(up) |
          reinterpret_cast<uintptr_t>(uc)) % 16 == 0) {
-        // one CTA per SM without a register cap, two with a 128 cap, or two
-        // with the density queue in shared memory
-        const bool one = policy == SIMWAVE_POLICY_VEC_1CTA;
-        const bool qs = policy == SIMWAVE_POLICY_VEC_SMEMQ ||
-                        (policy == SIMWAVE_POLICY_AUTO && vd && L.r >= 3);
-#define SW_VEC(RR)                                                                             \
-    case RR:                                                                                   \
-        if (vd && qs) launch_vec<RR, true, 2, true>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
-        else if (vd && one) launch_vec<RR, true, 1, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
-        else if (vd) launch_vec<RR, true, 2, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
-        else if (one) launch_vec<RR, false, 1, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
-        else launch_vec<RR, false, 2, false>(un, uc, up, vel, den, damp, L, W, dt, dt2, ctx, st); \
+#define SW_VEC(RR)                                                                              \
+    case RR:                                                                                    \
+        if (vd) launch_vec_policy<RR, true>(policy, un, uc, up, vel, den, damp, L, W, ctx, st); \
+        else launch_vec_policy<RR, false>(policy, un, uc, up, vel, den, damp, L, W, ctx, st);   \
         return;
         switch (L.r) { SW_VEC(1) SW_VEC(2) SW_VEC(3) SW_VEC(4) }
 #undef SW_VEC

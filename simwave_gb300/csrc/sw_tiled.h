@@ -19,6 +19,8 @@ struct TiledContext {
     long long slot_stride = 0;
     int zero_box[6] = {0, 0, 0, 0, 0, 0};  // z0, z1, x0, x1, y0, y1 (empty)
     int* err = nullptr;
+    const float* coefC = nullptr;  // per-point coefficients (same layout as u)
+    const float* coefQ = nullptr;
 };
 
 // Encodes the descriptors; false when the layout or alignment does not suit
@@ -26,10 +28,16 @@ struct TiledContext {
 bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
                    long long nslots, long long slot_stride, const float* den);
 
+// `coefC` and `coefQ` are the per-point coefficients of form_coefficients.
 void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc,
-                  const float* up, const float* vel, const float* den,
-                  const float* damp, const Layout& L, const Weights<float>& W,
+                  const float* up, const float* coefC, const float* den,
+                  const float* coefQ, const Layout& L, const Weights<float>& W,
                   float dt, float dt2, cudaStream_t st);
+
+// C = (dt^2 v^2) / (1 + Q), Q = damp dt v^2 / 2, elementwise over n values,
+// with the reference's operation order (all IEEE round-to-nearest).
+void form_coefficients(const float* vel, const float* damp, float* C, float* Q,
+                       long long n, float dt, cudaStream_t st);
 
 // Largest box around the grid centre (interior indices) where `damp` is zero,
 // found and verified on the device; writes {z0, z1, x0, x1, y0, y1} into the

@@ -161,7 +161,7 @@ def test_repeated_calls_are_deterministic():
 
 
 POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3,
-            "vec_smemq": 4}
+            "vec_smemq": 4, "vec_2cta_rot": 5, "vec_1cta_rot": 6}
 
 
 @pytest.mark.parametrize("policy", list(POLICIES))
