@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <type_traits>
 #include <chrono>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -162,8 +163,20 @@ struct Arena {
     Buffer u, vel, den, damp, wavelet, rec;
     Buffer src_iv, src_val, src_off, rec_iv, rec_val, rec_off;
     Buffer scratch;
-    cudaStream_t stream = nullptr;
+    Buffer stage_in[2], stage_out[2];  // dense staging of one grid each
+    cudaStream_t stream = nullptr;     // time loop
+    cudaStream_t copy_in = nullptr;    // host -> device copies and repacks
+    cudaStream_t copy_out = nullptr;   // repacks and device -> host copies
+    bool host_access = false;  // kernels may address pageable host memory
     std::vector<cudaEvent_t> events;
+    cudaEvent_t event(size_t i) {
+        while (events.size() <= i) {
+            cudaEvent_t e;
+            SW_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            events.push_back(e);
+        }
+        return events[i];
+    }
 };
 
 static std::mutex g_mutex;  // serialises the host-pointer entries
@@ -174,6 +187,16 @@ static Arena& arena_for_current_device() {
     SW_CUDA(cudaGetDevice(&dev));
     Arena& a = g_arenas[dev];
     if (!a.stream) SW_CUDA(cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking));
+    if (!a.copy_in || !a.copy_out) {
+        // copies at the lowest priority: the time loop's blocks go first
+        int lo = 0, hi = 0;
+        SW_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        SW_CUDA(cudaStreamCreateWithPriority(&a.copy_in, cudaStreamNonBlocking, lo));
+        SW_CUDA(cudaStreamCreateWithPriority(&a.copy_out, cudaStreamNonBlocking, lo));
+        int pageable = 0;
+        SW_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+        a.host_access = pageable != 0;
+    }
     return a;
 }
 
@@ -201,6 +224,8 @@ struct Run {
     size_t begin, end, stride;
     T dt;
     unsigned flags;
+    // optional hooks around each time step's launches (host-entry copies)
+    std::function<void(size_t)> before_step, after_step;
 };
 
 template <typename T>
@@ -320,6 +345,7 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
         T* un = R.u + (size_t)S.steps[i].next * L.slot;
         const T* uc = R.u + (size_t)S.steps[i].cur * L.slot;
         const T* up = R.u + (size_t)S.steps[i].prev * L.slot;
+        if (R.before_step) R.before_step(i);
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i], st));
         launch_stencil<T, DIM, VD>(R, tctx, un, uc, up, st, &stats.stencil_variant);
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i + 1], st));
@@ -352,6 +378,7 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
             SW_LAUNCHED("record_receivers");
             stats.kernel_launches++;
         }
+        if (R.after_step) R.after_step(i);
     }
 }
 
@@ -464,26 +491,17 @@ struct HostArgs {
     size_t begin, end, order, nslots;
 };
 
+// Grid transfers of the host entries: one contiguous copy of the dense host
+// array into a dense device staging buffer, then a repack into the pitched
+// layout on the device (and the reverse), so that the host link runs at full
+// rate; two staging buffers per direction alternate.
 template <typename T>
-static void copy_grid_h2d(T* dst, const T* src, const Layout& L,
-                          cudaStream_t st, size_t* bytes) {
-    const size_t nf = (size_t)L.nfast();
-    const size_t rows = (size_t)(L.dim == 3 ? L.nz * L.nx : L.nz);
-    SW_CUDA(cudaMemcpy2DAsync(dst + L.lead, L.pitch * sizeof(T), src,
-                              nf * sizeof(T), nf * sizeof(T), rows,
-                              cudaMemcpyHostToDevice, st));
-    *bytes += rows * nf * sizeof(T);
-}
-
-template <typename T>
-static void copy_grid_d2h(T* dst, const T* src, const Layout& L,
-                          cudaStream_t st, size_t* bytes) {
-    const size_t nf = (size_t)L.nfast();
-    const size_t rows = (size_t)(L.dim == 3 ? L.nz * L.nx : L.nz);
-    SW_CUDA(cudaMemcpy2DAsync(dst, nf * sizeof(T), src + L.lead,
-                              L.pitch * sizeof(T), nf * sizeof(T), rows,
-                              cudaMemcpyDeviceToHost, st));
-    *bytes += rows * nf * sizeof(T);
+static void repack(T* dst, const T* src, const Layout& L, bool to_pitched,
+                   cudaStream_t st) {
+    const long long rows = L.dim == 3 ? L.nz * L.nx : L.nz;
+    repack_rows<T><<<(unsigned)std::min<long long>(rows, 65535), 256, 0, st>>>(
+        dst, src, rows, L.nfast(), L.pitch, L.lead, to_pitched);
+    SW_LAUNCHED("repack_rows");
 }
 
 template <typename T>
@@ -540,20 +558,105 @@ static double host_forward(const HostArgs<T>& A) {
     T* drec = (T*)ar.rec.ensure(std::max<size_t>(A.end * A.nrec * sizeof(T), 16));
 
     size_t h2d = 0, d2h = 0;
-    for (size_t j = 0; j < A.nslots; j++)
-        if (S.touched[j]) copy_grid_h2d(du + j * L.slot, A.u + j * L.nz * L.nx * L.ny, L, st, &h2d);
-    copy_grid_h2d(dvel, A.vel, L, st, &h2d);
-    if (A.vd) copy_grid_h2d(dden, A.den, L, st, &h2d);
-    copy_grid_h2d(ddamp, A.damp, L, st, &h2d);
+    const size_t dense = (size_t)(L.nz * L.nx * L.ny);
+    const size_t dense_bytes = dense * sizeof(T);
+    T* sin[2] = {nullptr, nullptr};
+    T* sout[2] = {nullptr, nullptr};
+    if (!ar.host_access)
+        for (int b = 0; b < 2; b++) {
+            sin[b] = (T*)ar.stage_in[b].ensure(dense_bytes);
+            sout[b] = (T*)ar.stage_out[b].ensure(dense_bytes);
+        }
+    cudaStream_t cin = ar.copy_in, cout = ar.copy_out;
+    // events: [0,2) staging-in free, [2,4) staging-out free, [4] fields
+    // ready, [5, 5 + nslots) slot ready, [5 + nslots, 5 + 2 nslots) slot done
+    const size_t EV_IN = 0, EV_OUT = 2, EV_FIELDS = 4, EV_READY = 5;
+    const size_t EV_DONE = EV_READY + A.nslots;
+    ar.event(EV_DONE + A.nslots);
+    SW_CUDA(cudaEventRecord(ar.event(EV_IN), cin));
+    SW_CUDA(cudaEventRecord(ar.event(EV_IN + 1), cin));
+    SW_CUDA(cudaEventRecord(ar.event(EV_OUT), cout));
+    SW_CUDA(cudaEventRecord(ar.event(EV_OUT + 1), cout));
+    int in_turn = 0, out_turn = 0;
+    // with pageable-memory access the repack kernel reads/writes the host
+    // arrays itself (asynchronous, no staging); otherwise one contiguous
+    // copy per grid through the staging buffers
+    const bool direct = ar.host_access;
+    auto upload_grid = [&](T* dst, const T* src) {
+        h2d += dense_bytes;
+        if (direct) {
+            repack<T>(dst, src, L, true, cin);
+            return;
+        }
+        const int b = in_turn++ & 1;
+        SW_CUDA(cudaStreamWaitEvent(cin, ar.event(EV_IN + b), 0));
+        SW_CUDA(cudaMemcpyAsync(sin[b], src, dense_bytes, cudaMemcpyHostToDevice, cin));
+        repack<T>(dst, sin[b], L, true, cin);
+        SW_CUDA(cudaEventRecord(ar.event(EV_IN + b), cin));
+    };
+    auto download_grid = [&](T* dst, const T* src) {
+        d2h += dense_bytes;
+        if (direct) {
+            repack<T>(dst, src, L, false, cout);
+            return;
+        }
+        const int b = out_turn++ & 1;
+        SW_CUDA(cudaStreamWaitEvent(cout, ar.event(EV_OUT + b), 0));
+        repack<T>(sout[b], src, L, false, cout);
+        SW_CUDA(cudaMemcpyAsync(dst, sout[b], dense_bytes, cudaMemcpyDeviceToHost, cout));
+        SW_CUDA(cudaEventRecord(ar.event(EV_OUT + b), cout));
+    };
+    // models and KWS tables first, then the slots in the order the steps
+    // first touch them
+    upload_grid(dvel, A.vel);
+    if (A.vd) upload_grid(dden, A.den);
+    upload_grid(ddamp, A.damp);
     const size_t wlen = A.wavelet_size * std::max<size_t>(A.wavelet_count, 1);
-    T* dw = (T*)upload<T>(ar.wavelet, A.wavelet, A.nsrc ? wlen * sizeof(T) : 0, st, &h2d);
-    size_t* dsiv = (size_t*)upload<T>(ar.src_iv, A.src_iv, A.nsrc * 2 * A.dim * sizeof(size_t), st, &h2d);
-    T* dsval = (T*)upload<T>(ar.src_val, A.src_val, A.nsrc ? A.src_val_size * sizeof(T) : 0, st, &h2d);
-    size_t* dsoff = (size_t*)upload<T>(ar.src_off, A.src_off, A.nsrc ? A.nsrc * sizeof(size_t) : 0, st, &h2d);
-    size_t* driv = (size_t*)upload<T>(ar.rec_iv, A.rec_iv, A.nrec * 2 * A.dim * sizeof(size_t), st, &h2d);
-    T* drval = (T*)upload<T>(ar.rec_val, A.rec_val, A.nrec ? A.rec_val_size * sizeof(T) : 0, st, &h2d);
-    size_t* droff = (size_t*)upload<T>(ar.rec_off, A.rec_off, A.nrec ? A.nrec * sizeof(size_t) : 0, st, &h2d);
-
+    T* dw = (T*)upload<T>(ar.wavelet, A.wavelet, A.nsrc ? wlen * sizeof(T) : 0, cin, &h2d);
+    size_t* dsiv = (size_t*)upload<T>(ar.src_iv, A.src_iv, A.nsrc * 2 * A.dim * sizeof(size_t), cin, &h2d);
+    T* dsval = (T*)upload<T>(ar.src_val, A.src_val, A.nsrc ? A.src_val_size * sizeof(T) : 0, cin, &h2d);
+    size_t* dsoff = (size_t*)upload<T>(ar.src_off, A.src_off, A.nsrc ? A.nsrc * sizeof(size_t) : 0, cin, &h2d);
+    size_t* driv = (size_t*)upload<T>(ar.rec_iv, A.rec_iv, A.nrec * 2 * A.dim * sizeof(size_t), cin, &h2d);
+    T* drval = (T*)upload<T>(ar.rec_val, A.rec_val, A.nrec ? A.rec_val_size * sizeof(T) : 0, cin, &h2d);
+    size_t* droff = (size_t*)upload<T>(ar.rec_off, A.rec_off, A.nrec ? A.nrec * sizeof(size_t) : 0, cin, &h2d);
+    SW_CUDA(cudaEventRecord(ar.event(EV_FIELDS), cin));
+    // physical slot p starts with host slot p; upload those the run reads or
+    // returns, in first-use order
+    std::vector<size_t> first_use(A.nslots, (size_t)-1), last_write(A.nslots, (size_t)-1);
+    for (size_t i = 0; i < S.steps.size(); i++) {
+        const int ps[3] = {S.steps[i].prev, S.steps[i].cur, S.steps[i].next};
+        for (int q = 0; q < 3; q++)
+            if (first_use[ps[q]] == (size_t)-1) first_use[ps[q]] = i;
+        last_write[S.steps[i].next] = i;
+    }
+    std::vector<int> inv(A.nslots);
+    for (size_t j = 0; j < A.nslots; j++) inv[S.perm[j]] = (int)j;
+    std::vector<char> needed(A.nslots, 0), uploaded(A.nslots, 0);
+    for (size_t p = 0; p < A.nslots; p++)
+        needed[p] = first_use[p] != (size_t)-1 || inv[p] != (int)p;
+    std::vector<size_t> order;
+    for (size_t p = 0; p < A.nslots; p++)
+        if (needed[p]) order.push_back(p);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return first_use[a] < first_use[b]; });
+    for (size_t p : order) {
+        upload_grid(du + p * L.slot, A.u + p * dense);
+        SW_CUDA(cudaEventRecord(ar.event(EV_READY + p), cin));
+        uploaded[p] = 1;
+    }
+    // the time loop waits for the models, and for each slot before its
+    // first use; a slot's result leaves as soon as its last write is queued
+    SW_CUDA(cudaStreamWaitEvent(st, ar.event(EV_FIELDS), 0));
+    std::vector<std::vector<int>> start_at(S.steps.size() + 1), done_at(S.steps.size() + 1);
+    for (size_t p = 0; p < A.nslots; p++) {
+        if (first_use[p] != (size_t)-1) start_at[first_use[p]].push_back((int)p);
+        if (last_write[p] != (size_t)-1) done_at[last_write[p]].push_back((int)p);
+    }
+    auto emit = [&](int p) {  // result of physical slot p -> host slot inv[p]
+        SW_CUDA(cudaEventRecord(ar.event(EV_DONE + p), st));
+        SW_CUDA(cudaStreamWaitEvent(cout, ar.event(EV_DONE + p), 0));
+        download_grid(A.u + (size_t)inv[p] * dense, du + (size_t)p * L.slot);
+    };
     Run<T> R;
     R.L = L;
     R.vd = A.vd;
@@ -575,14 +678,22 @@ static double host_forward(const HostArgs<T>& A) {
     R.stride = A.stride;
     R.dt = A.dt;
     R.flags = 0;
+    R.before_step = [&](size_t i) {
+        for (int p : start_at[i]) SW_CUDA(cudaStreamWaitEvent(st, ar.event(EV_READY + p), 0));
+    };
+    // a slot's final content is known once the step after its last write has
+    // been queued (that step may still read it, which does not change it)
+    R.after_step = [&](size_t i) {
+        for (int p : done_at[i]) emit(p);
+    };
     dispatch_steps<T>(R, S, st, stats, nullptr);
 
-    // results: every slot that may have changed, and the receiver rows written
-    for (size_t j = 0; j < A.nslots; j++) {
-        const int phys = S.perm[j];
-        if (S.written[phys] || phys != (int)j)
-            copy_grid_d2h(A.u + j * L.nz * L.nx * L.ny, du + (size_t)phys * L.slot, L, st, &d2h);
-    }
+    // slots that changed identity without being written
+    for (size_t p = 0; p < A.nslots; p++)
+        if (last_write[p] == (size_t)-1 && inv[p] != (int)p) {
+            SW_CUDA(cudaStreamWaitEvent(st, ar.event(EV_READY + p), 0));
+            emit((int)p);
+        }
     if (rec_rows && A.nrec) {
         const size_t off = (A.begin - 1) * A.nrec;
         SW_CUDA(cudaMemcpyAsync(A.receivers + off, drec + off,
@@ -591,6 +702,8 @@ static double host_forward(const HostArgs<T>& A) {
         d2h += rec_rows * A.nrec * sizeof(T);
     }
     SW_CUDA(cudaStreamSynchronize(st));
+    SW_CUDA(cudaStreamSynchronize(cin));
+    SW_CUDA(cudaStreamSynchronize(cout));
     check_device_words(st);
     const double secs =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

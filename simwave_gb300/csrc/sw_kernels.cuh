@@ -220,4 +220,24 @@ __global__ void boundary_phase(T* __restrict__ u, Layout L, int axis,
     apply_edge(u, first, step, r, after, +1);
 }
 
+// ---- layout conversion: dense rows <-> pitched rows -----------------------
+// `rows` rows of `width` elements; dense row r at src + r * width, pitched
+// row r at dst + r * pitch + lead (to_pitched), or the reverse.
+template <typename T>
+__global__ void repack_rows(T* __restrict__ dst, const T* __restrict__ src,
+                            long long rows, long long width, long long pitch,
+                            long long lead, bool to_pitched) {
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        if (to_pitched) {
+            const T* s = src + r * width;
+            T* d = dst + r * pitch + lead;
+            for (long long c = threadIdx.x; c < width; c += blockDim.x) d[c] = s[c];
+        } else {
+            const T* s = src + r * pitch + lead;
+            T* d = dst + r * width;
+            for (long long c = threadIdx.x; c < width; c += blockDim.x) d[c] = s[c];
+        }
+    }
+}
+
 }  // namespace sw
