@@ -258,6 +258,19 @@ int simwave_forward_device(const simwave_problem *problem, void *stream);
 #define SIMWAVE_POLICY_VEC_1CTA_ROT 6   /* same, 1 CTA per SM */
 int simwave_set_kernel_policy(int policy);
 
+/* How the host-pointer entries move grids (process-wide).
+ * AUTO: page-lock the caller's grids for the duration of the call and copy
+ *   them with asynchronous pitched DMA (falls back to STAGED if locking
+ *   fails); STAGED: one contiguous pageable copy per grid through a device
+ *   staging buffer, repacked on the device; DIRECT: kernels read and write
+ *   the caller's pageable arrays (devices with pageable-memory access only,
+ *   else STAGED). Grid snapshots leave while the time loop is still running.
+ * No reference counterpart. */
+#define SIMWAVE_TRANSFER_AUTO 0
+#define SIMWAVE_TRANSFER_STAGED 1
+#define SIMWAVE_TRANSFER_DIRECT 2
+int simwave_set_transfer_mode(int mode);
+
 /* Wait for `stream` and report device-side failures of the forward calls
  * enqueued on it (a bounded wait that expired: SIMWAVE_E_TIMEOUT). Clears
  * the recorded status. No reference counterpart. */

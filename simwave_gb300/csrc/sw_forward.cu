@@ -180,6 +180,7 @@ struct Arena {
 };
 
 static std::mutex g_mutex;  // serialises the host-pointer entries
+static int g_transfer_mode = SIMWAVE_TRANSFER_AUTO;
 static std::map<int, Arena> g_arenas;
 
 static Arena& arena_for_current_device() {
@@ -504,6 +505,27 @@ static void repack(T* dst, const T* src, const Layout& L, bool to_pitched,
     SW_LAUNCHED("repack_rows");
 }
 
+// Page-locks caller arrays for the duration of one call (released by the
+// destructor); ranges already locked by the caller are used as they are.
+struct HostPins {
+    std::vector<void*> mine;
+    bool add(const void* p, size_t bytes) {
+        if (!p || !bytes) return true;
+        cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
+        if (e == cudaSuccess) {
+            mine.push_back(const_cast<void*>(p));
+            return true;
+        }
+        cudaGetLastError();  // clear
+        return e == cudaErrorHostMemoryAlreadyRegistered;
+    }
+    void release() {
+        for (void* p : mine) cudaHostUnregister(p);
+        mine.clear();
+    }
+    ~HostPins() { release(); }
+};
+
 template <typename T>
 static void* upload(Buffer& b, const void* src, size_t bytes, cudaStream_t st,
                     size_t* counted) {
@@ -560,13 +582,6 @@ static double host_forward(const HostArgs<T>& A) {
     size_t h2d = 0, d2h = 0;
     const size_t dense = (size_t)(L.nz * L.nx * L.ny);
     const size_t dense_bytes = dense * sizeof(T);
-    T* sin[2] = {nullptr, nullptr};
-    T* sout[2] = {nullptr, nullptr};
-    if (!ar.host_access)
-        for (int b = 0; b < 2; b++) {
-            sin[b] = (T*)ar.stage_in[b].ensure(dense_bytes);
-            sout[b] = (T*)ar.stage_out[b].ensure(dense_bytes);
-        }
     cudaStream_t cin = ar.copy_in, cout = ar.copy_out;
     // events: [0,2) staging-in free, [2,4) staging-out free, [4] fields
     // ready, [5, 5 + nslots) slot ready, [5 + nslots, 5 + 2 nslots) slot done
@@ -581,9 +596,33 @@ static double host_forward(const HostArgs<T>& A) {
     // with pageable-memory access the repack kernel reads/writes the host
     // arrays itself (asynchronous, no staging); otherwise one contiguous
     // copy per grid through the staging buffers
-    const bool direct = ar.host_access;
+    // transfer mode: pin the caller's grids in place for the call and let
+    // the copy engines move them with pitched DMA (AUTO), or let kernels
+    // address the pageable arrays directly (DIRECT, coherent host links), or
+    // one contiguous copy per grid through device staging (STAGED)
+    HostPins pins;
+    bool pinned = false;
+    if (g_transfer_mode == SIMWAVE_TRANSFER_AUTO) {
+        pinned = pins.add(A.u, dense_bytes * A.nslots) && pins.add(A.vel, dense_bytes) &&
+                 pins.add(A.damp, dense_bytes) && (!A.vd || pins.add(A.den, dense_bytes));
+        if (!pinned) pins.release();
+    }
+    const bool direct = !pinned && ar.host_access && g_transfer_mode == SIMWAVE_TRANSFER_DIRECT;
+    T* sin[2] = {nullptr, nullptr};
+    T* sout[2] = {nullptr, nullptr};
+    if (!direct && !pinned)
+        for (int b = 0; b < 2; b++) {
+            sin[b] = (T*)ar.stage_in[b].ensure(dense_bytes);
+            sout[b] = (T*)ar.stage_out[b].ensure(dense_bytes);
+        }
+    const size_t nf = (size_t)L.nfast(), rows = dense / nf;
     auto upload_grid = [&](T* dst, const T* src) {
         h2d += dense_bytes;
+        if (pinned) {
+            SW_CUDA(cudaMemcpy2DAsync(dst + L.lead, L.pitch * sizeof(T), src, nf * sizeof(T),
+                                      nf * sizeof(T), rows, cudaMemcpyHostToDevice, cin));
+            return;
+        }
         if (direct) {
             repack<T>(dst, src, L, true, cin);
             return;
@@ -596,6 +635,11 @@ static double host_forward(const HostArgs<T>& A) {
     };
     auto download_grid = [&](T* dst, const T* src) {
         d2h += dense_bytes;
+        if (pinned) {
+            SW_CUDA(cudaMemcpy2DAsync(dst, nf * sizeof(T), src + L.lead, L.pitch * sizeof(T),
+                                      nf * sizeof(T), rows, cudaMemcpyDeviceToHost, cout));
+            return;
+        }
         if (direct) {
             repack<T>(dst, src, L, false, cout);
             return;
@@ -1033,6 +1077,13 @@ extern "C" int simwave_set_kernel_policy(int policy) {
     if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_1CTA_ROT)
         return SIMWAVE_E_ARGUMENT;
     sw::set_kernel_policy(policy);
+    return SIMWAVE_OK;
+}
+
+extern "C" int simwave_set_transfer_mode(int mode) {
+    if (mode < SIMWAVE_TRANSFER_AUTO || mode > SIMWAVE_TRANSFER_DIRECT) return SIMWAVE_E_ARGUMENT;
+    std::lock_guard<std::mutex> lock(sw::g_mutex);
+    sw::g_transfer_mode = mode;
     return SIMWAVE_OK;
 }
 
