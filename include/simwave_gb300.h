@@ -276,6 +276,30 @@ int simwave_set_transfer_mode(int mode);
  * the recorded status. No reference counterpart. */
 int simwave_device_status(void *stream);
 
+/* ---- allocation-free variant -------------------------------------------
+ * simwave_forward_device_noalloc runs the same float32 3D forward as
+ * simwave_forward_device on caller-owned device arrays, but allocates no
+ * device memory at all: no cudaMalloc, cudaFree or allocating library call.
+ * It exists for callers that cannot let us allocate while they run: a host
+ * framework that owns the device memory budget through its own pool, a
+ * serving loop in which an allocation would synchronise the device and stall
+ * unrelated work, or code that enqueues work while a stream is captured.
+ * Its scratch (two per-point coefficient grids and 256 bytes of status
+ * words) lives in one file-scope device array of
+ * SIMWAVE_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
+ * until the process exits. Limits: 3D float32 problems only; a grid of at
+ * most (SIMWAVE_NOALLOC_SCRATCH_BYTES - 256) / 8 pitched points (larger grids
+ * are refused with SIMWAVE_E_ARGUMENT and a simwave_last_error() message);
+ * no SIMWAVE_FLAG_TIME_KERNELS; the layout must suit the tiled kernel (the
+ * one simwave_layout() returns does). The first call on a device looks up
+ * the array's device address (with that device current); make it before any
+ * stream capture. The call waits for `stream` before returning. All calls
+ * share the one array and its status words are reset at the start of each
+ * call: calls that overlap on the GPU race on it and must be serialised.
+ * No reference counterpart. */
+#define SIMWAVE_NOALLOC_SCRATCH_BYTES (32u << 20)
+int simwave_forward_device_noalloc(const simwave_problem *problem, void *stream);
+
 /* Statistics of the calling thread's last successful forward call. */
 typedef struct simwave_stats {
     double seconds;           /* wall time of the call */

@@ -36,6 +36,10 @@ static thread_local simwave_stats g_last_stats;
     throw Failure{code, msg};
 }
 
+// Sets the calling thread's simwave_last_error() message (for entry points
+// defined in other translation units).
+void record_error(const std::string& message) { g_last_error = message; }
+
 #define SW_CUDA(expr)                                                       \
     do {                                                                    \
         cudaError_t e_ = (expr);                                            \
