@@ -107,6 +107,97 @@ def config2_arguments(timesteps=None, n=384, stride=50):
     return kw
 
 
+def smooth_velocity(shape, rng, lo=1500.0, hi=4500.0, modes=6):
+    """Seeded smooth random field in [lo, hi]: a few low-wavenumber modes."""
+    z = np.linspace(0.0, 1.0, shape[0])[:, None]
+    x = np.linspace(0.0, 1.0, shape[1])[None, :]
+    f = np.zeros(shape)
+    for _ in range(modes):
+        kz, kx = rng.uniform(0.5, 3.0, size=2)
+        pz, px = rng.uniform(0, 2 * np.pi, size=2)
+        f += rng.uniform(0.3, 1.0) * np.sin(2 * np.pi * kz * z + pz) * np.cos(
+            2 * np.pi * kx * x + px)
+    f = (f - f.min()) / max(f.max() - f.min(), 1e-12)
+    return (lo + (hi - lo) * f).astype(np.float32)
+
+
+def config3_arguments(nshots=96, seed=7, max_side=2048):
+    """The batched workload: 2D constant-density shots with seeded grids of
+    256..max_side points per side (10 m), orders {4, 8, 12, 16, 20}, smooth
+    random velocity 1500-4500 m/s, 50-point damping layer, an 8-25 Hz Ricker
+    source and 256-1024 surface receivers, tf = 1.0 s."""
+    import simwave_gb300 as sw
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nshots):
+        nz, nx = (int(v) for v in rng.integers(256, max_side + 1, size=2))
+        order = int(rng.choice([4, 8, 12, 16, 20]))
+        h = 10.0
+        vel = smooth_velocity((nz, nx), rng)
+        sm = sw.SpaceModel((0, (nz - 1) * h, 0, (nx - 1) * h), (h, h), vel,
+                           space_order=order, dtype=np.float32)
+        sm.config_boundary(damping_length=50 * h, boundary_condition="none",
+                           damping_polynomial_degree=3, damping_alpha=0.001)
+        tm = sw.TimeModel(space_model=sm, tf=1.0, saving_stride=0)
+        xs = float(rng.uniform(0.2, 0.8) * (nx - 1) * h)
+        src = sw.Source(sm, coordinates=[(20.0, xs)], window_radius=4)
+        nrec = int(rng.integers(256, 1025))
+        rx = np.linspace(0.0, (nx - 1) * h, nrec)
+        rec = sw.Receiver(sm, coordinates=np.stack([np.full(nrec, 10.0), rx], 1),
+                          window_radius=4)
+        wav = sw.RickerWavelet(float(rng.uniform(8.0, 25.0)), tm)
+        out.append(sw.Solver(sm, tm, src, rec, wav).forward_arguments())
+    return out
+
+
+def batched_leg(nshots=96, max_side=2048):
+    """Shots/s of back-to-back single-shot runs vs one batch (resident)."""
+    import torch
+    from simwave_gb300.batch import BatchEngine, autotune, run_batch
+    from simwave_gb300.device import DeviceProblem
+    kws = config3_arguments(nshots, max_side=max_side)
+    probs = [DeviceProblem(k) for k in kws]
+    updates = sum(interior_updates(k)[1] for k in kws)
+    stream = torch.cuda.current_stream()
+    # plain: one simwave_forward_device call per shot, back to back
+    probs[0].run()
+    probs[0].status()
+    for p in probs:
+        p.reset()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for p in probs:
+        p.run(stream)
+    e1.record(stream)
+    e1.synchronize()
+    plain_s = e0.elapsed_time(e1) / 1e3
+    # batch: tile heights picked per order, then one engine for all shots
+    tiles = autotune(probs, steps=32)
+    eng = BatchEngine()
+    for order, rows in tiles.items():
+        eng.set_tile_rows(order, rows)
+    for p in probs:
+        p.reset()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    run_batch(probs, engine=eng)
+    e1.record(stream)
+    e1.synchronize()
+    batch_s = e0.elapsed_time(e1) / 1e3
+    launches = eng.launches()
+    eng.close()
+    return {"workload": "%d 2D CD shots, 256..%d per side, orders 4-20, tf 1 s"
+                        % (nshots, max_side),
+            "shots_per_s": round(nshots / batch_s, 2),
+            "plain_shots_per_s": round(nshots / plain_s, 2),
+            "speedup_vs_plain": round(plain_s / batch_s, 2),
+            "batch_gpts": round(updates / batch_s / 1e9, 2),
+            "plain_gpts": round(updates / plain_s / 1e9, 2),
+            "tile_rows": tiles, "batch_launches": int(launches),
+            "timing": "CUDA events, resident inputs, setup excluded"}
+
+
 def interior_updates(kw):
     shape = kw["velocity_model"].shape
     r = kw["space_order"] // 2
@@ -268,6 +359,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=384,
                     help="model points per axis (default 384)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 96-shot batched leg")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -365,6 +458,10 @@ def main():
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": round(e2e_total / len(e2e_ms), 3)}
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_leg()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, secs, threads = cpu_sample(args.cpu_steps, n=args.n)
@@ -397,6 +494,7 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clock_info,
             "cpu_baseline": cpu,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

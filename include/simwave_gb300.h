@@ -300,6 +300,35 @@ int simwave_device_status(void *stream);
 #define SIMWAVE_NOALLOC_SCRATCH_BYTES (32u << 20)
 int simwave_forward_device_noalloc(const simwave_problem *problem, void *stream);
 
+/* ---- batch engine: many 2D shots advanced together ------------------------
+ * Shots are 2D float32 problems on device-resident arrays (pitched layout of
+ * simwave_layout(), KWS windows already validated: SIMWAVE_FLAG_WINDOWS_CHECKED);
+ * the arrays must stay valid until the shot is released. Each step of the
+ * batch advances every unfinished shot by one time step with one launch per
+ * (order, density) group for the stencil and one per sparse term for all
+ * shots; the launch sequence of 16 steps is captured once as a CUDA graph and
+ * replayed while the shot set is unchanged. Results equal the single-shot
+ * entries' (same operator and schedule).
+ * No reference counterpart (the reference runs one shot per call). */
+typedef struct simwave_batch simwave_batch;
+int simwave_batch_create(simwave_batch **out);
+int simwave_batch_destroy(simwave_batch *batch);
+/* Add a shot (problem fields as for simwave_forward_device); writes its id. */
+int simwave_batch_add(simwave_batch *batch, const simwave_problem *problem,
+                      int *shot_id);
+/* Advance every unfinished shot by up to `steps` time steps, ordered after
+ * prior work on `stream`; `stream` waits for the batch. */
+int simwave_batch_run(simwave_batch *batch, int steps, void *stream);
+/* Time steps left for a shot (0 when finished). */
+int simwave_batch_remaining(simwave_batch *batch, int shot_id, int *steps);
+/* Remove a shot; a finished shot's slots are put back in the reference's
+ * order first. Waits for the batch's work. */
+int simwave_batch_release(simwave_batch *batch, int shot_id);
+/* Tuning: stencil tile height (8, 16 or 32 rows) for one space order. */
+int simwave_batch_set_tile_rows(simwave_batch *batch, int space_order, int rows);
+/* Kernel launches enqueued so far (graph nodes counted per replay). */
+int simwave_batch_launches(simwave_batch *batch, size_t *launches);
+
 /* Statistics of the calling thread's last successful forward call. */
 typedef struct simwave_stats {
     double seconds;           /* wall time of the call */

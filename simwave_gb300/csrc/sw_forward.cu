@@ -258,6 +258,14 @@ static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
                            int* variant) {
     const Layout& L = R.L;
     const T dt2 = R.dt * R.dt;
+    if constexpr (std::is_same<T, float>::value && DIM == 2) {
+        if (tctx.ok) {
+            tiled2d_launch(L, VD, un, uc, up, tctx.coefC, tctx.coefQ, R.den, R.W, st);
+            *variant = 1;
+            SW_LAUNCHED("stencil2d_single");
+            return;
+        }
+    }
     if constexpr (std::is_same<T, float>::value && DIM == 3) {
         if (tctx.ok) {
             tiled_launch(tctx, VD, un, uc, up, tctx.coefC, R.den, tctx.coefQ, L,
@@ -309,7 +317,20 @@ template <typename T>
 static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
     TiledContext ctx;
     if constexpr (std::is_same<T, float>::value) {
-        if (R.L.dim != 3 || (R.flags & SIMWAVE_FLAG_GENERIC_KERNEL)) return ctx;
+        if (R.flags & SIMWAVE_FLAG_GENERIC_KERNEL) return ctx;
+        if (R.L.dim == 2) {
+            if (!tiled2d_supported(R.L) ||
+                (reinterpret_cast<uintptr_t>(R.u) | reinterpret_cast<uintptr_t>(R.den)) % 16)
+                return ctx;
+            float* cq = coefficient_scratch((size_t)R.L.slot * 2);
+            const long long n = R.L.nz * R.L.pitch;
+            form_coefficients(R.vel, R.damp, cq, cq + R.L.slot, n, (float)R.dt, st);
+            SW_LAUNCHED("form_coefficients");
+            ctx.coefC = cq;
+            ctx.coefQ = cq + R.L.slot;
+            ctx.ok = true;
+            return ctx;
+        }
         if (!tiled_prepare(ctx, R.L, R.vd, R.u, (long long)R.nslots,
                            (long long)R.L.slot, R.den))
             return ctx;

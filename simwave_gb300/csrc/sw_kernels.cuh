@@ -127,23 +127,17 @@ __device__ __forceinline__ long long window_offset(const Layout& L,
     return L.at2(b[0] + iz, b[2] + ix);
 }
 
-// ---- sources: one block per source, threads over its window --------------
-// (constant_density/2d/wave.c:182-271). Overlapping windows of different
-// sources add through atomics, like the reference's `omp atomic`.
+// ---- sources: KWS injection of one source window ---------------------------
+// (constant_density/2d/wave.c:182-271): u_next += dt^2 v^2 kws w / D over the
+// window; threads t0, t0 + tstride, ... of the window. Overlapping windows of
+// different sources add through atomics, like the reference's `omp atomic`.
 template <typename T, int DIM>
-__global__ void inject_sources(T* __restrict__ un, const T* __restrict__ vel,
-                               const T* __restrict__ damp, Layout L,
-                               Windows<T> src, const T* __restrict__ wavelet,
-                               size_t wavelet_count, size_t n, T dt, T dt2) {
-    const size_t s = blockIdx.x;
-    if (s >= src.count) return;
-    const T w = wavelet_count > 1 ? wavelet[(n - 1) * src.count + s]
-                                  : wavelet[n - 1];
-    if (w == T(0)) return;
-    const size_t* b = src.interval + s * 2 * DIM;
-    const T* v = src.values + src.offsets[s];
+__device__ __forceinline__ void inject_window(T* un, const T* vel, const T* damp,
+                                              const Layout& L, const size_t* b,
+                                              const T* v, T w, T dt, T dt2, int t0,
+                                              int tstride) {
     const long long total = window_size<DIM>(b);
-    for (long long t = threadIdx.x; t < total; t += blockDim.x) {
+    for (long long t = t0; t < total; t += tstride) {
         long long iz, ix, iy;
         window_point<DIM>(b, t, iz, ix, iy);
         const T kws = window_weight<T, DIM>(b, v, iz, ix, iy);
@@ -154,8 +148,58 @@ __global__ void inject_sources(T* __restrict__ un, const T* __restrict__ vel,
     }
 }
 
-// ---- receivers: one warp per receiver, window sum by shuffles -------------
-// (constant_density/2d/wave.c:395-464); reads the current level.
+// Wavelet sample of source s at step n (wave.c:199-205).
+template <typename T>
+__device__ __forceinline__ T wavelet_at(const T* wavelet, size_t count, size_t n,
+                                        size_t nsrc, size_t s) {
+    return count > 1 ? wavelet[(n - 1) * nsrc + s] : wavelet[n - 1];
+}
+
+// One block per source, threads over its window.
+template <typename T, int DIM>
+__global__ void inject_sources(T* __restrict__ un, const T* __restrict__ vel,
+                               const T* __restrict__ damp, Layout L,
+                               Windows<T> src, const T* __restrict__ wavelet,
+                               size_t wavelet_count, size_t n, T dt, T dt2) {
+    const size_t s = blockIdx.x;
+    if (s >= src.count) return;
+    const T w = wavelet_at(wavelet, wavelet_count, n, src.count, s);
+    if (w == T(0)) return;
+    inject_window<T, DIM>(un, vel, damp, L, src.interval + s * 2 * DIM,
+                          src.values + src.offsets[s], w, dt, dt2, threadIdx.x,
+                          blockDim.x);
+}
+
+// ---- receivers: KWS gather of one receiver window by one warp --------------
+// (constant_density/2d/wave.c:395-464); reads the current level. Lanes take
+// the window's (z[, x]) rows; each row is summed along its contiguous axis;
+// the lane sums are reduced with shuffles. Returns the sum in every lane.
+template <typename T, int DIM>
+__device__ __forceinline__ T gather_window(const T* uc, const Layout& L, const size_t* b,
+                                           const T* v, int lane) {
+    const int lz = (int)(b[1] - b[0] + 1), lx = (int)(b[3] - b[2] + 1);
+    const int ly = DIM == 3 ? (int)(b[5] - b[4] + 1) : 1;
+    const int rows = DIM == 3 ? lz * lx : lz;
+    T sum = 0;
+    for (int row = lane; row < rows; row += 32) {
+        if (DIM == 3) {
+            const int iz = row / lx, ix = row - iz * lx;
+            const T wzx = v[iz] * v[lz + ix];
+            const T* vy = v + lz + lx;
+            const T* u = uc + L.at3(b[0] + iz, b[2] + ix, b[4]);
+            for (int iy = 0; iy < ly; iy++) sum += u[iy] * (wzx * vy[iy]);
+        } else {
+            const T wz = v[row];
+            const T* vx = v + lz;
+            const T* u = uc + L.at2(b[0] + row, b[2]);
+            for (int ix = 0; ix < lx; ix++) sum += u[ix] * (wz * vx[ix]);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    return sum;
+}
+
+// One warp per receiver.
 template <typename T, int DIM>
 __global__ void record_receivers(T* __restrict__ rec_row,
                                  const T* __restrict__ uc, Layout L,
@@ -163,21 +207,12 @@ __global__ void record_receivers(T* __restrict__ rec_row,
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= (long long)rec.count) return;
-    const size_t* b = rec.interval + warp * 2 * DIM;
-    const T* v = rec.values + rec.offsets[warp];
-    const long long total = window_size<DIM>(b);
-    T sum = 0;
-    for (long long t = lane; t < total; t += 32) {
-        long long iz, ix, iy;
-        window_point<DIM>(b, t, iz, ix, iy);
-        sum += uc[window_offset<DIM>(L, b, iz, ix, iy)] *
-               window_weight<T, DIM>(b, v, iz, ix, iy);
-    }
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    const T sum = gather_window<T, DIM>(uc, L, rec.interval + warp * 2 * DIM,
+                                        rec.values + rec.offsets[warp], lane);
     if (lane == 0) rec_row[warp] = sum;
 }
 
-// ---- boundary conditions: one thread per line normal to `axis` ------------
+// ---- boundary conditions: one line normal to `axis` --------------------------
 // Applies the before edge then the after edge of one axis, like one
 // iteration of the reference's BC loops (constant_density/2d/wave.c:274-393,
 // constant_density/3d/wave.c:299-481). Phases (axes) are separate launches
@@ -195,22 +230,24 @@ __device__ __forceinline__ void apply_edge(T* u, long long first,
     }
 }
 
+// Number of lines of the phase normal to `axis`.
+__host__ __device__ __forceinline__ long long boundary_lines(const Layout& L, int axis) {
+    const int a1 = axis == 0 ? 1 : 0;
+    const int a2 = L.dim == 3 ? (axis == 2 ? 1 : 2) : -1;
+    return (L.extent(a1) - 2 * L.r) * (a2 >= 0 ? L.extent(a2) - 2 * L.r : 1);
+}
+
+// Line t of the phase normal to `axis`.
 template <typename T>
-__global__ void boundary_phase(T* __restrict__ u, Layout L, int axis,
-                               int before, int after) {
+__device__ __forceinline__ void boundary_line(T* u, const Layout& L, int axis, int before,
+                                              int after, long long t) {
     const int r = L.r;
-    // the two other axes, in increasing index order
-    int a1 = axis == 0 ? 1 : 0;
-    int a2 = L.dim == 3 ? (axis == 2 ? 1 : 2) : -1;
-    const long long n1 = L.extent(a1) - 2 * r;
+    const int a1 = axis == 0 ? 1 : 0;  // the two other axes, increasing
+    const int a2 = L.dim == 3 ? (axis == 2 ? 1 : 2) : -1;
     const long long n2 = a2 >= 0 ? L.extent(a2) - 2 * r : 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n1 * n2) return;
-    const long long i1 = r + t / n2;
-    const long long i2 = a2 >= 0 ? r + t % n2 : 0;
     long long idx[3] = {0, 0, 0};
-    idx[a1] = i1;
-    if (a2 >= 0) idx[a2] = i2;
+    idx[a1] = r + t / n2;
+    if (a2 >= 0) idx[a2] = r + t % n2;
     const long long step = L.stride(axis);
     idx[axis] = r;
     long long first = L.dim == 3 ? L.at3(idx[0], idx[1], idx[2]) : L.at2(idx[0], idx[1]);
@@ -218,6 +255,14 @@ __global__ void boundary_phase(T* __restrict__ u, Layout L, int axis,
     idx[axis] = L.extent(axis) - r - 1;
     first = L.dim == 3 ? L.at3(idx[0], idx[1], idx[2]) : L.at2(idx[0], idx[1]);
     apply_edge(u, first, step, r, after, +1);
+}
+
+template <typename T>
+__global__ void boundary_phase(T* __restrict__ u, Layout L, int axis,
+                               int before, int after) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= boundary_lines(L, axis)) return;
+    boundary_line(u, L, axis, before, after, t);
 }
 
 // ---- layout conversion: dense rows <-> pitched rows -----------------------

@@ -42,6 +42,13 @@ void form_coefficients(const float* vel, const float* damp, float* C, float* Q,
 // Largest box around the grid centre (interior indices) where `damp` is zero,
 // found and verified on the device; writes {z0, z1, x0, x1, y0, y1} into the
 // device array `box` (7 ints: the 6 bounds and a verification word).
+// Tiled 2D float32 stencil of one shot (sw_batch.cu), on the per-point
+// coefficients of form_coefficients; 16-byte aligned pitched rows.
+bool tiled2d_supported(const Layout& L);
+void tiled2d_launch(const Layout& L, bool vd, float* un, const float* uc, const float* up,
+                    const float* C, const float* Q, const float* den,
+                    const Weights<float>& W, cudaStream_t st);
+
 int kernel_policy();
 void set_kernel_policy(int policy);
 

@@ -196,3 +196,26 @@ def test_tiled_and_generic_kernels_agree(order, vd, policy):
     assert_close(gen_u, ru, np.float32, "generic wavefield")
     assert_close(tiled_rec, rrec, np.float32, "tiled shot record")
     assert rel_l2(tiled_u, gen_u) < 2e-5
+
+
+@pytest.mark.parametrize("order", [2, 4, 8, 14, 20])
+@pytest.mark.parametrize("vd", [False, True])
+def test_tiled2d_and_generic_kernels_agree(order, vd):
+    """The tiled 2D kernel against the one-thread-per-point kernel and the
+    checker (partial tiles in both axes)."""
+    from simwave_gb300.device import DeviceProblem
+    bc = ("null_neumann", "null_dirichlet", "null_dirichlet", "null_neumann")
+    kw = random_problem(sw, 2, order, vd, bc, 3, shape=(77, 301), tf=0.04,
+                        seed=order, nrec=6)
+    dp = DeviceProblem(kw)
+    st = dp.run()
+    dp.status()
+    assert st["stencil_variant"] == 1, "tiled 2D kernel not selected"
+    tiled_u = dp.u_full_numpy()
+    dp.reset()
+    st = dp.run(generic=True)
+    assert st["stencil_variant"] == 0
+    gen_u = dp.u_full_numpy()
+    ru, rrec = port_forward(kw)
+    assert_close(tiled_u, ru, np.float32, "tiled 2D wavefield")
+    assert rel_l2(tiled_u, gen_u) < 2e-5
