@@ -56,6 +56,11 @@ struct Shot {
     float dt, dt2;
     int n, begin, end;     // next step to run, first and last step
     int bc[4];
+    int zb[4];             // z0, z1, x0, x1: box where Q is zero
+};
+
+struct ZeroBox2 {
+    int b[4];
 };
 
 struct TileRef {
@@ -85,7 +90,7 @@ __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, flo
                                                const float* uc, const float* up,
                                                const float* C, const float* Q,
                                                const float* den, const Weights<float>& W,
-                                               int tz, int tx) {
+                                               const int* zb, int tz, int tx) {
     constexpr int HX = (R + 3) & ~3;
     constexpr int TW = 128 + 2 * HX;   // floats per tile row
     constexpr int TH = TZ + 2 * R;     // tile rows
@@ -116,12 +121,42 @@ __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, flo
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int x = x0 + 4 * lane;            // first of this lane's 4 points
     const int xlim = (int)L.nx - R;         // interior x < xlim
+    const bool xbox = x >= zb[2] && x + 3 < zb[3];
     const float c20 = W.c2[0];
     for (int rr = warp; rr < TZ; rr += kWarps) {
         const int z = z0 + rr;
         if (z >= nz - R || x >= xlim) continue;
         const float* tu = tile + (rr + R) * TW + 4 * lane;      // row z, chunk start
         const float* tr = tile + TH * TW + (rr + R) * TW + 4 * lane;
+        const long long p = (long long)z * pitch + L.lead + x;
+        // partial chunks read into the next row (never the last row), masked below
+        const float4 cc = *reinterpret_cast<const float4*>(C + p);
+        const float4 pv = *reinterpret_cast<const float4*>(up + p);
+        const bool qzero = xbox && z >= zb[0] && z < zb[1];  // damping-free box
+        const float4 qq = qzero ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                : *reinterpret_cast<const float4*>(Q + p);
+        // z axis: rows z +- k of the tile, this lane's 4 columns
+        const float4 u0 = *reinterpret_cast<const float4*>(tu + HX);
+        float4 sz = make_float4(c20 * u0.x, c20 * u0.y, c20 * u0.z, c20 * u0.w);
+        float4 gz = make_float4(0.f, 0.f, 0.f, 0.f), rz = gz;
+#pragma unroll
+        for (int k = 1; k <= R; k++) {
+            const float4 a = *reinterpret_cast<const float4*>(tu + k * TW + HX);
+            const float4 b = *reinterpret_cast<const float4*>(tu - k * TW + HX);
+            const float c = W.c2[k];
+            sz.x = fmaf(c, a.x + b.x, sz.x); sz.y = fmaf(c, a.y + b.y, sz.y);
+            sz.z = fmaf(c, a.z + b.z, sz.z); sz.w = fmaf(c, a.w + b.w, sz.w);
+            if (VD) {
+                const float d = W.c1[k];
+                gz.x = fmaf(d, a.x - b.x, gz.x); gz.y = fmaf(d, a.y - b.y, gz.y);
+                gz.z = fmaf(d, a.z - b.z, gz.z); gz.w = fmaf(d, a.w - b.w, gz.w);
+                const float4 ra = *reinterpret_cast<const float4*>(tr + k * TW + HX);
+                const float4 rb = *reinterpret_cast<const float4*>(tr - k * TW + HX);
+                rz.x = fmaf(d, ra.x - rb.x, rz.x); rz.y = fmaf(d, ra.y - rb.y, rz.y);
+                rz.z = fmaf(d, ra.z - rb.z, rz.z); rz.w = fmaf(d, ra.w - rb.w, rz.w);
+            }
+        }
+        // x axis: this lane's window of 4 + 2 HX values
         float wu[4 + 2 * HX], wr[VD ? 4 + 2 * HX : 1];
 #pragma unroll
         for (int c = 0; c < (4 + 2 * HX) / 4; c++) {
@@ -132,40 +167,34 @@ __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, flo
                 wr[4 * c] = b.x; wr[4 * c + 1] = b.y; wr[4 * c + 2] = b.z; wr[4 * c + 3] = b.w;
             }
         }
-        float out[4];
-        const long long p = (long long)z * pitch + L.lead + x;
-        // partial chunks read into the next row (never the last row), masked below
-        const float4 cc = *reinterpret_cast<const float4*>(C + p);
-        const float4 qq = *reinterpret_cast<const float4*>(Q + p);
-        const float4 pv = *reinterpret_cast<const float4*>(up + p);
+        const float sza[4] = {sz.x, sz.y, sz.z, sz.w};
+        const float gza[4] = {gz.x, gz.y, gz.z, gz.w};
+        const float rza[4] = {rz.x, rz.y, rz.z, rz.w};
         const float ca[4] = {cc.x, cc.y, cc.z, cc.w};
         const float qa[4] = {qq.x, qq.y, qq.z, qq.w};
         const float pa[4] = {pv.x, pv.y, pv.z, pv.w};
+        float out[4];
 #pragma unroll
         for (int v = 0; v < 4; v++) {
-            const float u0 = wu[HX + v];
-            float sx = c20 * u0, sz = c20 * u0, gx = 0.f, gz = 0.f, rx = 0.f, rz = 0.f;
+            const float uu = wu[HX + v];
+            float sx = c20 * uu, gx = 0.f, rx = 0.f;
 #pragma unroll
             for (int k = 1; k <= R; k++) {
                 const float xp = wu[HX + v + k], xm = wu[HX + v - k];
-                const float zp = tu[k * TW + HX + v], zm = tu[-k * TW + HX + v];
                 sx = fmaf(W.c2[k], xp + xm, sx);
-                sz = fmaf(W.c2[k], zp + zm, sz);
                 if (VD) {
                     gx = fmaf(W.c1[k], xp - xm, gx);
-                    gz = fmaf(W.c1[k], zp - zm, gz);
                     rx = fmaf(W.c1[k], wr[HX + v + k] - wr[HX + v - k], rx);
-                    rz = fmaf(W.c1[k], tr[k * TW + HX + v] - tr[-k * TW + HX + v], rz);
                 }
             }
             // reference order: x then z (constant_density/2d/wave.c:166)
-            float lap = sx * W.ih2[1] + sz * W.ih2[0];
+            float lap = sx * W.ih2[1] + sza[v] * W.ih2[0];
             if (VD) {
-                const float cross = gx * rx * W.s1[1] + gz * rz * W.s1[0];
+                const float cross = gx * rx * W.s1[1] + gza[v] * rza[v] * W.s1[0];
                 lap -= __fdividef(cross, wr[HX + v]);
             }
             const float q = qa[v];
-            const float a = fmaf(-(1.f - q), pa[v], 2.f * u0);
+            const float a = fmaf(-(1.f - q), pa[v], 2.f * uu);
             const float b = q == 0.f ? a : a * __fdividef(1.f, 1.f + q);
             out[v] = fmaf(lap, ca[v], b);
         }
@@ -193,7 +222,7 @@ stencil2d_batched(const Shot* __restrict__ shots, const TileRef* __restrict__ ti
     slot_ptrs(S, un, uc, up);
     const Layout L = S.L;
     stencil2d_tile<R, VD, TZ>(reinterpret_cast<float*>(sw_batch_smem), L, un, uc, up, S.C,
-                              S.Q, S.den, S.W, t.tz, t.tx);
+                              S.Q, S.den, S.W, S.zb, t.tz, t.tx);
 }
 
 // One shot: grid (x tiles, z tiles).
@@ -201,9 +230,9 @@ template <int R, bool VD, int TZ>
 __global__ void __launch_bounds__(kThreads)
 stencil2d_single(Layout L, float* un, const float* __restrict__ uc, const float* up,
                  const float* __restrict__ C, const float* __restrict__ Q,
-                 const float* __restrict__ den, Weights<float> W) {
+                 const float* __restrict__ den, Weights<float> W, ZeroBox2 zb) {
     stencil2d_tile<R, VD, TZ>(reinterpret_cast<float*>(sw_batch_smem), L, un, uc, up, C, Q,
-                              den, W, blockIdx.y, blockIdx.x);
+                              den, W, zb.b, blockIdx.y, blockIdx.x);
 }
 
 // ---- batched sparse terms --------------------------------------------------------
@@ -343,7 +372,7 @@ static void launch_group(bool configure, int r, bool vd, int tz, const Shot* sho
 template <int R, bool VD>
 static void single_r(const Layout& L, float* un, const float* uc, const float* up,
                      const float* C, const float* Q, const float* den,
-                     const Weights<float>& W, cudaStream_t st) {
+                     const Weights<float>& W, const int* box, cudaStream_t st) {
     constexpr int TZ = 16, HX = (R + 3) & ~3;
     const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
     static bool configured[64] = {};
@@ -354,7 +383,8 @@ static void single_r(const Layout& L, float* un, const float* uc, const float* u
         configured[dev & 63] = true;
     }
     dim3 grid((unsigned)((L.nx - 2 * R + 127) / 128), (unsigned)((L.nz - 2 * R + TZ - 1) / TZ));
-    stencil2d_single<R, VD, TZ><<<grid, kThreads, bytes, st>>>(L, un, uc, up, C, Q, den, W);
+    ZeroBox2 zb{{box[0], box[1], box[2], box[3]}};
+    stencil2d_single<R, VD, TZ><<<grid, kThreads, bytes, st>>>(L, un, uc, up, C, Q, den, W, zb);
 }
 
 struct Engine {
@@ -648,7 +678,19 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
                             cudaMemcpyHostToDevice, E.stream));
     form_coefficients(d.vel, d.damp, h.cq, h.cq + grid, grid, d.dt, E.stream);
     SB_CUDA(cudaGetLastError());
-    SB_CUDA(cudaStreamSynchronize(E.stream));
+    // box where Q is zero (its loads are skipped there)
+    int* words = nullptr;
+    SB_CUDA(cudaMalloc(&words, 8 * sizeof(int)));
+    find_zero_box(h.cq + grid, d.L, words, E.stream);
+    int box[7];
+    const cudaError_t copied =
+        cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, E.stream);
+    const cudaError_t synced = cudaStreamSynchronize(E.stream);
+    cudaFree(words);
+    SB_CUDA(copied);
+    SB_CUDA(synced);
+    const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
+    for (int i = 0; i < 4; i++) d.zb[i] = good ? box[i] : 0;
     d.C = h.cq;
     d.Q = h.cq + grid;
     d.slots = h.slots;
@@ -712,11 +754,11 @@ bool tiled2d_supported(const Layout& L) {
 
 void tiled2d_launch(const Layout& L, bool vd, float* un, const float* uc, const float* up,
                     const float* C, const float* Q, const float* den,
-                    const Weights<float>& W, cudaStream_t st) {
+                    const Weights<float>& W, const int* zero_box, cudaStream_t st) {
 #define SB_S(RR)                                                                          \
     case RR:                                                                              \
-        if (vd) batch::single_r<RR, true>(L, un, uc, up, C, Q, den, W, st);              \
-        else batch::single_r<RR, false>(L, un, uc, up, C, Q, den, W, st);                \
+        if (vd) batch::single_r<RR, true>(L, un, uc, up, C, Q, den, W, zero_box, st);    \
+        else batch::single_r<RR, false>(L, un, uc, up, C, Q, den, W, zero_box, st);      \
         break;
     switch (L.r) {
         SB_S(1) SB_S(2) SB_S(3) SB_S(4) SB_S(5) SB_S(6) SB_S(7) SB_S(8) SB_S(9) SB_S(10)

@@ -260,7 +260,8 @@ static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
     const T dt2 = R.dt * R.dt;
     if constexpr (std::is_same<T, float>::value && DIM == 2) {
         if (tctx.ok) {
-            tiled2d_launch(L, VD, un, uc, up, tctx.coefC, tctx.coefQ, R.den, R.W, st);
+            tiled2d_launch(L, VD, un, uc, up, tctx.coefC, tctx.coefQ, R.den, R.W,
+                           tctx.zero_box, st);
             *variant = 1;
             SW_LAUNCHED("stencil2d_single");
             return;
@@ -328,6 +329,15 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
             SW_LAUNCHED("form_coefficients");
             ctx.coefC = cq;
             ctx.coefQ = cq + R.L.slot;
+            int* words = device_words();
+            find_zero_box(ctx.coefQ, R.L, words, st);
+            SW_LAUNCHED("find_zero_box");
+            int box[7];
+            SW_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
+            SW_CUDA(cudaStreamSynchronize(st));
+            const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
+            for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
+            ctx.err = words + 7;
             ctx.ok = true;
             return ctx;
         }

@@ -748,7 +748,7 @@ void launch_r(float* un, const float* uc, const float* up, const float* vel, con
 }
 
 // Walk each axis line through the grid centre outwards while the mask is
-// zero; one thread per axis.
+// zero; one thread per axis (in 2D the y range is [0, 1)).
 __global__ void zero_box_lines(const float* __restrict__ damp, Layout L, int* box) {
     const int a = threadIdx.x;
     if (a >= 3) return;
@@ -757,7 +757,7 @@ __global__ void zero_box_lines(const float* __restrict__ damp, Layout L, int* bo
     auto at = [&](long long i) {
         long long idx[3] = {c[0], c[1], c[2]};
         idx[a] = i;
-        return damp[L.at3(idx[0], idx[1], idx[2])];
+        return damp[L.dim == 3 ? L.at3(idx[0], idx[1], idx[2]) : L.at2(idx[0], idx[1])];
     };
     long long lo = c[a], hi = c[a];
     if (at(c[a]) != 0.f) {
@@ -782,7 +782,7 @@ __global__ void zero_box_verify(const float* __restrict__ damp, Layout L, int* b
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         const long long k = t % nyb, j = (t / nyb) % nxb, i = t / (nyb * nxb);
-        bad |= damp[L.at3(z0 + i, x0 + j, y0 + k)] != 0.f;
+        bad |= damp[L.dim == 3 ? L.at3(z0 + i, x0 + j, y0 + k) : L.at2(z0 + i, x0 + j)] != 0.f;
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(box + 6, 1);
 }

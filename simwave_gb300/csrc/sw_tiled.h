@@ -45,9 +45,10 @@ void form_coefficients(const float* vel, const float* damp, float* C, float* Q,
 // Tiled 2D float32 stencil of one shot (sw_batch.cu), on the per-point
 // coefficients of form_coefficients; 16-byte aligned pitched rows.
 bool tiled2d_supported(const Layout& L);
+// `zero_box` (z0, z1, x0, x1) bounds points where Q is known to be zero.
 void tiled2d_launch(const Layout& L, bool vd, float* un, const float* uc, const float* up,
                     const float* C, const float* Q, const float* den,
-                    const Weights<float>& W, cudaStream_t st);
+                    const Weights<float>& W, const int* zero_box, cudaStream_t st);
 
 int kernel_policy();
 void set_kernel_policy(int policy);
