@@ -198,6 +198,95 @@ def batched_leg(nshots=96, max_side=2048):
             "timing": "CUDA events, resident inputs, setup excluded"}
 
 
+def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320):
+    """The served workload: Poisson arrivals (seeded, ``rate`` per second) of
+    2D shots (512..max2d per side) and 3D shots (128..max3d per side), orders
+    4-16, float32, constant or Gardner density, tf 0.5-2.0 s, 10 m grids,
+    30-point damping layer, one source, surface receivers."""
+    import simwave_gb300 as sw
+    from simwave_gb300.serve import Request
+    rng = np.random.default_rng(seed)
+    reqs, t = [], 0.0
+    for i in range(nreq):
+        t += float(rng.exponential(1.0 / rate))
+        is3d = rng.random() < frac3d
+        order = int(rng.choice([4, 6, 8, 10, 12, 14, 16]))
+        gardner = bool(rng.integers(0, 2))
+        tf = float(rng.uniform(0.5, 2.0))
+        h = 10.0
+        if is3d:
+            n = int(rng.integers(128, max3d + 1))
+            shape = (n, n, n)
+            z = np.linspace(0, 1, n, dtype=np.float32)[:, None, None]
+            vel = np.broadcast_to(1500 + 2500 * z, shape).astype(np.float32)
+            vel = vel * (1 + 0.05 * np.sin(np.linspace(0, 6, n, dtype=np.float32))[None, :, None])
+        else:
+            shape = tuple(int(v) for v in rng.integers(512, max2d + 1, size=2))
+            vel = smooth_velocity(shape, rng)
+        vel = vel.astype(np.float32)
+        den = (310.0 * vel ** 0.25).astype(np.float32) if gardner else None
+        box = []
+        for a in range(len(shape)):
+            box += [0.0, (shape[a] - 1) * h]
+        sm = sw.SpaceModel(tuple(box), (h,) * len(shape), vel, den, space_order=order,
+                           dtype=np.float32)
+        sm.config_boundary(damping_length=30 * h, boundary_condition="none")
+        tm = sw.TimeModel(space_model=sm, tf=tf, saving_stride=0)
+        mid = [(shape[a] - 1) * h / 2 for a in range(len(shape))]
+        src = sw.Source(sm, coordinates=[[20.0] + mid[1:]], window_radius=4)
+        if is3d:
+            g = np.linspace(0, (shape[1] - 1) * h, 32)
+            gx, gy = np.meshgrid(g, g, indexing="ij")
+            coords = np.stack([np.full(gx.size, 10.0), gx.ravel(), gy.ravel()], 1)
+        else:
+            coords = np.stack([np.full(256, 10.0), np.linspace(0, (shape[1] - 1) * h, 256)], 1)
+        rec = sw.Receiver(sm, coordinates=coords, window_radius=4)
+        wav = sw.RickerWavelet(float(rng.uniform(8.0, 20.0)), tm)
+        kw = sw.Solver(sm, tm, src, rec, wav).forward_arguments()
+        reqs.append(Request(kw, t, tag=i))
+    return reqs
+
+
+def served_leg(nreq=40):
+    """p50/p99 latency and shots/s of the continuous-batching server against
+    the same requests run one after another through the drop-in host path."""
+    import contextlib
+    import io
+    import torch
+    from simwave_gb300.backend.middleware import Middleware
+    from simwave_gb300.serve import ShotServer, latency_summary
+    reqs = config4_requests(nreq)
+    arrivals = [r.arrival for r in reqs]
+    updates = sum(interior_updates(r.kwargs)[1] for r in reqs)
+    # sequential: Solver.forward's host path, one request at a time
+    mw = Middleware()
+    service = []
+    for r in reqs:
+        k = dict(r.kwargs, u_full=np.zeros_like(r.kwargs["u_full"]),
+                 shot_record=np.zeros_like(r.kwargs["shot_record"]))
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(io.StringIO()):
+            mw.exec("forward", **k)
+        service.append(time.perf_counter() - t0)
+    done, lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        done = max(done, a) + sv
+        lat.append(done - a)
+    seq = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
+           "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
+           "shots_per_s": round(len(reqs) / (done - arrivals[0]), 2)}
+    # served: continuous batching
+    torch.cuda.synchronize()
+    server = ShotServer(epoch_steps=64)
+    server.serve(reqs)
+    server.close()
+    served = latency_summary(reqs)
+    return {"workload": "%d requests, Poisson 200/s, 2D 512^2-2048^2 and 3D 128^3-320^3, "
+                        "orders 4-16, tf 0.5-2 s" % len(reqs),
+            "updates": updates, "served": served, "sequential_plain": seq,
+            "speedup_shots_per_s": round(served["shots_per_s"] / seq["shots_per_s"], 2)}
+
+
 def interior_updates(kw):
     shape = kw["velocity_model"].shape
     r = kw["space_order"] // 2
@@ -361,10 +450,18 @@ def main():
                     help="model points per axis (default 384)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 96-shot batched leg")
+    ap.add_argument("--served", action="store_true",
+                    help="run only the served (continuous batching) leg")
     args = ap.parse_args()
 
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+
+    if args.served:
+        import torch
+        print(json.dumps({"metric": "served p50/p99 latency and shots/s",
+                          **served_leg()}), flush=True)
         return
 
     world, rank, local = dist_setup(args.gpus)

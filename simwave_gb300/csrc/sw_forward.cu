@@ -303,68 +303,58 @@ static int* device_words() {
     return w;
 }
 
-// Scratch for the per-point coefficients of the tiled kernels (floats).
-static float* coefficient_scratch(size_t count) {
-    static std::mutex m;
-    static std::map<int, Buffer> bufs;
-    int dev = 0;
-    SW_CUDA(cudaGetDevice(&dev));
-    std::lock_guard<std::mutex> lock(m);
-    return (float*)bufs[dev].ensure(count * sizeof(float));
-}
-
-// Tiled-kernel context of one run (float32 3D only).
+// Tiled-kernel context of one run (float32): per-point coefficients C, Q and
+// the zero-box words in scratch allocated on the run's stream (stream-ordered,
+// so concurrent runs on different streams never share it), freed by
+// release_tiled when the run's launches are queued.
 template <typename T>
 static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
     TiledContext ctx;
     if constexpr (std::is_same<T, float>::value) {
         if (R.flags & SIMWAVE_FLAG_GENERIC_KERNEL) return ctx;
-        if (R.L.dim == 2) {
-            if (!tiled2d_supported(R.L) ||
+        const Layout& L = R.L;
+        if (L.dim == 2) {
+            if (!tiled2d_supported(L) ||
                 (reinterpret_cast<uintptr_t>(R.u) | reinterpret_cast<uintptr_t>(R.den)) % 16)
                 return ctx;
-            float* cq = coefficient_scratch((size_t)R.L.slot * 2);
-            const long long n = R.L.nz * R.L.pitch;
-            form_coefficients(R.vel, R.damp, cq, cq + R.L.slot, n, (float)R.dt, st);
-            SW_LAUNCHED("form_coefficients");
-            ctx.coefC = cq;
-            ctx.coefQ = cq + R.L.slot;
-            int* words = device_words();
-            find_zero_box(ctx.coefQ, R.L, words, st);
-            SW_LAUNCHED("find_zero_box");
-            int box[7];
-            SW_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
-            SW_CUDA(cudaStreamSynchronize(st));
-            const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
-            for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
-            ctx.err = words + 7;
-            ctx.ok = true;
+        } else if (!tiled_prepare(ctx, L, R.vd, R.u, (long long)R.nslots, (long long)L.slot,
+                                  R.den)) {
             return ctx;
         }
-        if (!tiled_prepare(ctx, R.L, R.vd, R.u, (long long)R.nslots,
-                           (long long)R.L.slot, R.den))
-            return ctx;
-        // per-point coefficients C, Q in library scratch (grow-only, per device)
-        float* cq = coefficient_scratch((size_t)R.L.slot * 2);
-        float* C = cq;
-        float* Q = cq + R.L.slot;
-        const long long n = R.L.dim == 3 ? R.L.nz * R.L.plane : R.L.nz * R.L.pitch;
-        form_coefficients(R.vel, R.damp, C, Q, n, (float)R.dt, st);
+        ctx.ok = false;
+        const size_t n = (size_t)(L.dim == 3 ? L.nz * L.plane : L.nz * L.pitch);
+        void* scratch = nullptr;
+        SW_CUDA(cudaMallocAsync(&scratch, 2 * n * sizeof(float) + 16 * sizeof(int), st));
+        ctx.scratch = scratch;
+        float* C = static_cast<float*>(scratch);
+        float* Q = C + n;
+        int* words = reinterpret_cast<int*>(Q + n);
+        form_coefficients(R.vel, R.damp, C, Q, (long long)n, (float)R.dt, st);
         SW_LAUNCHED("form_coefficients");
-        ctx.coefC = C;
-        ctx.coefQ = Q;
-        int* words = device_words();
-        find_zero_box(Q, R.L, words, st);
+        find_zero_box(Q, L, words, st);
         SW_LAUNCHED("find_zero_box");
         int box[7];
         SW_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
         SW_CUDA(cudaStreamSynchronize(st));
-        const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2] && box[5] > box[4];
+        bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
+        if (L.dim == 3) good = good && box[5] > box[4];
         for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
-        ctx.err = words + 7;
+        ctx.coefC = C;
+        ctx.coefQ = Q;
+        ctx.err = device_words() + 7;
+        ctx.ok = true;
     }
     return ctx;
 }
+
+// Frees a run's stream-ordered scratch after its last launch.
+struct ScratchRelease {
+    void* p;
+    cudaStream_t st;
+    ~ScratchRelease() {
+        if (p) cudaFreeAsync(p, st);
+    }
+};
 
 template <typename T, int DIM, bool VD>
 static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
@@ -376,6 +366,7 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
     if (DIM == 3) { phases[0] = 2; phases[1] = 1; phases[2] = 0; nphase = 3; }
     else { phases[0] = 1; phases[1] = 0; nphase = 2; }
     const TiledContext tctx = prepare_tiled<T>(R, st);
+    ScratchRelease release{tctx.scratch, st};
     for (size_t i = 0; i < S.steps.size(); i++) {
         const size_t n = R.begin + i;
         T* un = R.u + (size_t)S.steps[i].next * L.slot;
@@ -913,15 +904,11 @@ static int device_forward(const simwave_problem* P, cudaStream_t st) {
     bool moved = false;
     for (size_t j = 0; j < P->num_snapshots; j++) moved |= S.perm[j] != (int)j;
     if (moved) {
-        int dev = 0;
-        SW_CUDA(cudaGetDevice(&dev));
-        Buffer* scratch;
-        {
-            std::lock_guard<std::mutex> lock(g_mutex);
-            scratch = &g_arenas[dev].scratch;
-        }
         const size_t bytes = grid_elems * sizeof(T);
-        T* tmp = (T*)scratch->ensure(bytes);
+        void* tmpv = nullptr;
+        SW_CUDA(cudaMallocAsync(&tmpv, bytes, st));
+        ScratchRelease tmp_release{tmpv, st};
+        T* tmp = static_cast<T*>(tmpv);
         std::vector<char> done(P->num_snapshots, 0);
         T* base = (T*)P->u;
         for (size_t j = 0; j < P->num_snapshots; j++) {

@@ -21,6 +21,7 @@ struct TiledContext {
     int* err = nullptr;
     const float* coefC = nullptr;  // per-point coefficients (same layout as u)
     const float* coefQ = nullptr;
+    void* scratch = nullptr;       // the run's coefficient/zero-box scratch
 };
 
 // Encodes the descriptors; false when the layout or alignment does not suit

@@ -238,6 +238,13 @@ class DeviceProblem:
         if status != 0:
             raise RuntimeError("device status {}: {}".format(status, _lib.last_error()))
 
+    def release_inputs(self):
+        """Drop the device copies of the models and tables; the wavefield
+        slots and the shot record stay."""
+        self.vel = self.den = self.damp = self.wavelet = None
+        self.src_iv = self.src_val = self.src_off = None
+        self.rec_iv = self.rec_val = self.rec_off = None
+
     def u_full_numpy(self):
         return self.u.cpu().numpy()
 

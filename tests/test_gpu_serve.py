@@ -1,0 +1,75 @@
+"""Continuous-batching server: every request's result is the same served in
+a mix (2D batched with other shots, 3D overlapping on streams, admission
+gated by the HBM budget) as run alone."""
+import numpy as np
+import pytest
+
+import simwave_gb300 as sw
+from _cases import random_problem, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(seed=1, count=10):
+    from simwave_gb300.serve import Request
+    rng = np.random.default_rng(seed)
+    reqs, arrival = [], 0.0
+    for i in range(count):
+        dim = 3 if rng.random() < 0.3 else 2
+        order = int(rng.choice([4, 8, 12, 16]))
+        vd = bool(rng.integers(0, 2))
+        if dim == 2:
+            shape = tuple(int(v) for v in rng.integers(60, 200, size=2))
+        else:
+            shape = tuple(int(v) for v in rng.integers(24, 40, size=3))
+            if vd:
+                shape = (shape[0], shape[1], shape[1])
+        kw = random_problem(sw, dim, order, vd, "none", int(rng.integers(0, 3)),
+                            shape=shape, tf=float(rng.uniform(0.03, 0.08)),
+                            seed=seed * 100 + i, nrec=int(rng.integers(2, 9)))
+        arrival += float(rng.exponential(1 / 200.0))
+        reqs.append(Request(kw, arrival, tag=i))
+    return reqs
+
+
+def _alone(kw):
+    from simwave_gb300.device import DeviceProblem
+    dp = DeviceProblem(kw)
+    dp.run()
+    dp.status()
+    return dp.u_full_numpy(), dp.shot_record_numpy()
+
+
+def test_served_results_equal_alone():
+    from simwave_gb300.serve import ShotServer, latency_summary
+    reqs = _requests()
+    server = ShotServer(epoch_steps=16)
+    server.serve(reqs, timeout=300)
+    server.close()
+    for r in reqs:
+        u, rec = _alone(r.kwargs)
+        assert not r.evicted
+        assert rel_l2(r.problem.u_full_numpy(), u) <= 1e-5, r.tag
+        assert rel_l2(r.shot_record, rec) <= 1e-5, r.tag
+    s = latency_summary(reqs)
+    assert s["shots"] == len(reqs) and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_budget_gates_admission():
+    from simwave_gb300.serve import ShotServer
+    reqs = _requests(seed=4, count=6)
+    budget = max(r.bytes for r in reqs) + 1
+    server = ShotServer(hbm_budget=budget, epoch_steps=8)
+    peak = []
+    orig = server._admit
+
+    def admit(now):
+        out = orig(now)
+        peak.append(server.in_use - server.resident)
+        return out
+
+    server._admit = admit
+    server.serve(reqs, timeout=300)
+    server.close()
+    assert all(r.completed is not None for r in reqs)
+    assert max(peak) <= budget
