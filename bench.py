@@ -287,6 +287,112 @@ def served_leg(nreq=40):
             "speedup_shots_per_s": round(served["shots_per_s"] / seq["shots_per_s"], 2)}
 
 
+def config5_models(seed=5):
+    """The inversion workload's models on a (351, 1701) grid of 10 m (nz = 351,
+    nx = 1701): 12 layers from 1500 to 5500 m/s cut by two dipping faults
+    (seeded), and its Gaussian smoothing with sigma = 20 points (the model
+    the gradient is evaluated at)."""
+    from scipy.ndimage import gaussian_filter
+    nz, nx = 351, 1701
+    rng = np.random.default_rng(seed)
+    z = np.arange(nz, dtype=np.float64)[:, None]
+    x = np.arange(nx, dtype=np.float64)[None, :]
+    depths = np.sort(rng.uniform(15.0, 340.0, 11))
+    speeds = np.clip(np.linspace(1500.0, 5500.0, 12) + rng.uniform(-80.0, 80.0, 12),
+                     1500.0, 5500.0)
+    speeds[0], speeds[-1] = 1500.0, 5500.0
+    shift = np.zeros((nz, nx))
+    for x0, dip, throw in ((520.0, 62.0, 24.0), (1180.0, 71.0, -31.0)):
+        trace = x0 + z / np.tan(np.radians(dip))
+        shift += np.where(x > trace, throw, 0.0)
+    layer = np.searchsorted(depths, z - shift)
+    true = speeds[layer].astype(np.float32)
+    smooth = gaussian_filter(true.astype(np.float64), 20.0, mode="nearest").astype(np.float32)
+    return true, smooth
+
+
+def config5_arguments(vel, dt=None, nshots=16, damping_points=50):
+    """Middleware keyword arguments of the inversion shots on ``vel``: so 8,
+    8 Hz Ricker, tf 3.0 s, sources at 20 m depth spread over x, 1701
+    receivers at 10 m depth (one per grid column), a 50-point damping layer
+    (deg 3, alpha 0.001) and 'none' edges. ``dt`` overrides the CFL step
+    (the observed and modelled data share the true model's step)."""
+    import simwave_gb300 as sw
+    nz, nx = vel.shape
+    h = 10.0
+    sm = sw.SpaceModel((0.0, (nz - 1) * h, 0.0, (nx - 1) * h), (h, h), vel,
+                       space_order=8, dtype=np.float32)
+    sm.config_boundary(damping_length=damping_points * h, boundary_condition="none",
+                       damping_polynomial_degree=3, damping_alpha=0.001)
+    tm = sw.TimeModel(space_model=sm, tf=3.0, dt=dt, saving_stride=0)
+    rec = sw.Receiver(sm, coordinates=[(10.0, i * h) for i in range(nx)], window_radius=4)
+    wav = sw.RickerWavelet(8.0, tm)
+    out = []
+    for s in range(nshots):
+        xs = (s + 0.5) * (nx - 1) * h / nshots
+        src = sw.Source(sm, coordinates=[(20.0, xs)], window_radius=4)
+        out.append(sw.Solver(sm, tm, src, rec, wav).forward_arguments())
+    return out, float(tm.dt)
+
+
+def gradient_leg(nshots=16, steps=1, interval=None):
+    """The inversion workload: L2 misfit and its velocity gradient over the
+    shots at the smoothed model, observed data from the true model. Reports
+    shots/s, the point updates of the forward, recomputation and adjoint
+    passes per second, and a finite-difference check of the gradient along
+    a random smooth direction on the first shot."""
+    import torch
+    from simwave_gb300.device import DeviceProblem
+    from simwave_gb300.gradient import default_interval, misfit_gradient, shot_record
+    true, smooth = config5_models()
+    kw_true, dt = config5_arguments(true, nshots=nshots)
+    kw_model, _ = config5_arguments(smooth, dt=dt, nshots=nshots)
+    observed = []
+    for kw in kw_true:
+        p = DeviceProblem(kw)
+        p.run()
+        observed.append(p.receivers[:, :p.nrec].clone())
+        del p
+    problems = [DeviceProblem(kw) for kw in kw_model]
+    v0 = torch.tensor(kw_model[0]["velocity_model"], device="cuda")
+    T = problems[0].timesteps
+    K = interval or default_interval(T)
+    misfit_gradient(v0, problems[:1], observed[:1], K)  # warm-up
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        loss, grad = misfit_gradient(v0, problems, observed, K)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    best = min(times)
+    _, interior = interior_updates(kw_model[0])
+    interior //= T
+    # finite differences of the misfit of shot 0 along a smooth direction
+    rng = np.random.default_rng(0)
+    from scipy.ndimage import gaussian_filter
+    d = gaussian_filter(rng.standard_normal(v0.shape), 15.0)
+    d = torch.tensor((50.0 * d / np.abs(d).max()).astype(np.float32), device="cuda")
+    _, g0 = misfit_gradient(v0, problems[:1], observed[:1], K)
+
+    def misfit(v):
+        with torch.no_grad():
+            rec = shot_record(v, problems[0], K)
+            return 0.5 * float(torch.sum((rec.double() - observed[0].double()) ** 2))
+
+    eps = 0.5
+    fd = (misfit(v0 + eps * d) - misfit(v0 - eps * d)) / (2 * eps)
+    ad = float(torch.sum(g0.double() * d.double()))
+    return {"workload": "%d shots, (351+pad)x(1701+pad) grid (nz 351, nx 1701, 10 m), "
+                        "so 8, 8 Hz Ricker, 1701 receivers, tf 3.0 s, T %d, "
+                        "checkpoint interval %d" % (nshots, T, K),
+            "grid": list(problems[0].shape), "timesteps": T, "interval": K,
+            "seconds": round(best, 4), "shots_per_s": round(nshots / best, 3),
+            "gpts_per_s_3pass": round(3.0 * nshots * interior * T / best / 1e9, 2),
+            "misfit": loss, "fd_directional": fd, "adjoint_directional": ad,
+            "fd_rel_diff": abs(fd - ad) / abs(fd)}
+
+
 def interior_updates(kw):
     shape = kw["velocity_model"].shape
     r = kw["space_order"] // 2
@@ -452,10 +558,17 @@ def main():
                     help="skip the 96-shot batched leg")
     ap.add_argument("--served", action="store_true",
                     help="run only the served (continuous batching) leg")
+    ap.add_argument("--gradient", action="store_true",
+                    help="run only the inversion (velocity gradient) leg")
     args = ap.parse_args()
 
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+
+    if args.gradient:
+        print(json.dumps({"metric": "FWI misfit gradient shots/s",
+                          **gradient_leg(steps=args.steps)}), flush=True)
         return
 
     if args.served:

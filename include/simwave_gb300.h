@@ -343,6 +343,43 @@ typedef struct simwave_stats {
 /* No reference counterpart (the reference returns only its wall time). */
 int simwave_last_stats(simwave_stats *out);
 
+/* ---- velocity gradient (2D, float32, constant density) ------------------
+ * No reference counterpart: the reference offers only the forward operator
+ * (simwave/kernel/backend/compiler.py:128-130) and its middleware dispatches
+ * only 'forward' (simwave/kernel/backend/middleware.py:103-105).
+ *
+ * The gradient is that of J = sum(g * receivers) with respect to the
+ * velocity grid, for a cotangent g of the shot record, through the exact
+ * discrete forward loop (damping, KWS source and receiver windows, boundary
+ * conditions), with dt, the damping mask and the windows held fixed. The
+ * forward starts from zero levels; `u`, `num_snapshots`, `saving_stride` and
+ * `slot_stride` are not used. KWS windows must lie inside the interior
+ * (SIMWAVE_E_ARGUMENT otherwise), and each interior extent must be at least
+ * space_order + 2. All work is ordered on `stream`; the calls copy the KWS
+ * windows to the host (a stream synchronisation) and allocate their scratch
+ * on the stream (cudaMallocAsync). */
+
+/* Number of grids (nz * pitch float32 elements each) the checkpoint buffer
+ * of a run with checkpoint `interval` steps needs: 2 * ceil(steps / interval). */
+int simwave_gradient_checkpoints(const simwave_problem *problem, size_t interval,
+                                 size_t *grids);
+
+/* Forward pass: writes the shot record into `receivers` (row n-1 from level
+ * n, as simwave_forward_device) and the level pair (u^(n-1), u^n) before
+ * every `interval`-th step into `checkpoints` (device). */
+int simwave_gradient_forward(const simwave_problem *problem, size_t interval,
+                             void *checkpoints, void *stream);
+
+/* Reverse pass: from the checkpoints of simwave_gradient_forward (same
+ * problem and interval) and `grad_receivers` (device, end_timestep rows of
+ * num_receivers float32), writes dJ/dv into `grad_velocity` (device, one
+ * grid in the problem's pitched layout; zero outside the interior). Needs
+ * (interval + 8) grids of scratch, plus interval rows of the Dirichlet
+ * lines when an edge is null_dirichlet. */
+int simwave_gradient_backward(const simwave_problem *problem, size_t interval,
+                              const void *checkpoints, const void *grad_receivers,
+                              void *grad_velocity, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -646,18 +646,9 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
     d.vel = (const float*)P->velocity;
     d.damp = (const float*)P->damp;
     d.den = vd ? (const float*)P->density : nullptr;
-    const float* c2 = (const float*)P->coeff_order2;
-    const float* c1 = vd ? (const float*)P->coeff_order1 : nullptr;
-    for (int k = 0; k <= r; k++) {
-        d.W.c2[k] = c2[k];
-        d.W.c1[k] = c1 ? c1[k] : 0.f;
-    }
-    const double hh[2] = {P->dz, P->dx};
-    for (int a = 0; a < 2; a++) {
-        const float h2 = (float)hh[a] * (float)hh[a];
-        d.W.ih2[a] = (float)(1.0 / (double)h2);
-        d.W.s1[a] = (float)(1.0 / (4.0 * (double)h2));
-    }
+    d.W = make_weights<float>((const float*)P->coeff_order2,
+                              vd ? (const float*)P->coeff_order1 : nullptr, r, P->dz,
+                              P->dx, 1.0);
     d.src = Windows<float>{P->src_points_interval, (const float*)P->src_points_values,
                            P->src_points_values_offset, P->num_sources};
     d.rec = Windows<float>{P->rec_points_interval, (const float*)P->rec_points_values,

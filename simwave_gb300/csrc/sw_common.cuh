@@ -12,6 +12,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 
 namespace sw {
 
@@ -66,6 +67,27 @@ struct Weights {
     T ih2[3];              // per axis (z, x, y): 1 / h^2
     T s1[3];               // per axis 1 / (4 h^2) (variable density cross term)
 };
+
+// Weights of one problem: the half weights as given (c1 only for variable
+// density) and, per axis, 1/h^2 and 1/(4 h^2) with h^2 formed in the model
+// precision like the reference's `dz * dz`.
+template <typename T>
+inline Weights<T> make_weights(const T* c2, const T* c1, int r, double dz, double dx,
+                               double dy) {
+    Weights<T> W;
+    std::memset(&W, 0, sizeof(W));
+    const double h[3] = {dz, dx, dy};
+    for (int k = 0; k <= r; k++) {
+        W.c2[k] = c2[k];
+        W.c1[k] = c1 ? c1[k] : T(0);
+    }
+    for (int a = 0; a < 3; a++) {
+        const T h2 = (T)h[a] * (T)h[a];
+        W.ih2[a] = (T)(1.0 / (double)h2);
+        W.s1[a] = (T)(1.0 / (4.0 * (double)h2));
+    }
+    return W;
+}
 
 // Ragged KWS windows of a set of sources or receivers, in the reference's
 // layout (source.py:123-159): per entry 2*dim interval ends, concatenated

@@ -233,25 +233,6 @@ struct Run {
     std::function<void(size_t)> before_step, after_step;
 };
 
-template <typename T>
-static Weights<T> make_weights(const T* c2, const T* c1, int r, double dz,
-                               double dx, double dy) {
-    Weights<T> W;
-    std::memset(&W, 0, sizeof(W));
-    const double h[3] = {dz, dx, dy};
-    for (int k = 0; k <= r; k++) {
-        W.c2[k] = c2[k];
-        W.c1[k] = c1 ? c1[k] : T(0);
-    }
-    for (int a = 0; a < 3; a++) {
-        // h^2 as the reference forms it: in the model precision
-        const T h2 = (T)h[a] * (T)h[a];
-        W.ih2[a] = (T)(1.0 / (double)h2);
-        W.s1[a] = (T)(1.0 / (4.0 * (double)h2));
-    }
-    return W;
-}
-
 template <typename T, int DIM, bool VD>
 static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
                            const T* uc, const T* up, cudaStream_t st,

@@ -1,0 +1,610 @@
+// sw_gradient.cu -- velocity gradient of the 2D float32 constant-density
+// forward loop: a forward pass that keeps checkpoints and a reverse pass that
+// recomputes one segment of levels at a time and runs the discrete adjoint.
+//
+// The reference has no adjoint (its compiler offers only the forward
+// operator, simwave/kernel/backend/compiler.py:128-130). The forward step n
+// (constant_density/2d/wave.c) is
+//   w       = (2 u^n - N u^(n-1)) / D + C (L u^n + s_n)   interior points
+//   u^(n+1) = B w              boundary conditions (x edges, then z edges)
+//   rec[n-1] = R u^n           KWS gather of the current level
+// with D = 1 + q, N = 1 - q, q = damp dt v^2 / 2, C = dt^2 v^2 / D. For a
+// cotangent g of the shot record, the adjoint of w at level m, scaled by C,
+//   nu^m = C * B^T [ R^T g[m-1] + (2/D) mu^(m+1) - (N/D) mu^(m+2) + L^T (C mu^(m+1)) ],
+//   mu = nu / C,
+// is, written out, the forward update itself applied to nu with a zero halo
+//   nu^m = (2 nu^(m+1) - N nu^(m+2)) / D + C L nu^(m+1)  (+ C R^T g[m-1]),
+// followed by the transposed boundary operations (z edges, then x edges):
+// a Dirichlet zero stays a zero; a Neumann copy u[halo] = u[mirror] becomes
+// nu[mirror] += C[mirror] * (L nu^(m+1))[halo]. So the reverse pass runs the
+// forward's own stencil on the adjoint levels. The velocity derivative of w,
+// (2 v / D^2) (dt^2 (L u^n + s_n) - damp dt (u^n - u^(n-1))), becomes
+// 2 (w^(n+1) - 2 u^n + u^(n-1)) / (D v) once the update is substituted for
+// dt^2 (L u^n + s_n); with mu = nu / C the gradient is
+//   dJ/dv = sum_m nu^m * 2 / (v^3 dt^2) * (w^m - 2 u^(m-1) + u^(m-2)),
+// where w^m equals u^m except on the Dirichlet lines, whose values before
+// the boundary conditions are saved during the recomputation.
+//
+// Checkpoints: the pair (u^(n-1), u^n) before every `interval`-th step,
+// stored by the forward pass in a caller buffer; the reverse pass rebuilds
+// `interval` levels from each pair, last segment first.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "simwave_gb300.h"
+#include "sw_kernels.cuh"
+#include "sw_tiled.h"
+
+namespace sw {
+
+void record_error(const std::string& message);
+
+namespace grad {
+
+struct Refusal {
+    int code;
+    std::string message;
+};
+
+[[noreturn]] static void refuse(int code, const std::string& m) { throw Refusal{code, m}; }
+
+#define GR_CUDA(expr)                                                               \
+    do {                                                                            \
+        cudaError_t e_ = (expr);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            ::sw::grad::refuse(e_ == cudaErrorMemoryAllocation ? SIMWAVE_E_MEMORY   \
+                                                               : SIMWAVE_E_CUDA,    \
+                               std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define GR_LAUNCHED(name)                                                          \
+    do {                                                                           \
+        cudaError_t e_ = cudaGetLastError();                                       \
+        if (e_ != cudaSuccess)                                                     \
+            ::sw::grad::refuse(SIMWAVE_E_CUDA, std::string("launch ") + name + ": " + \
+                                                   cudaGetErrorString(e_));        \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// kernels
+
+// K = 2 / (v^3 dt^2): the velocity factor of the gradient.
+__global__ void gradient_factor(const float* __restrict__ vel, float* __restrict__ K,
+                                long long n, float dt) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float v = vel[i];
+        K[i] = 2.0f / (v * v * v * (dt * dt));
+    }
+}
+
+// The ring of interior points next to the halo (the Dirichlet lines): the
+// rows z = r and z = nz-r-1 over the interior columns, then the columns
+// x = r and x = nx-r-1 over the rows strictly between those two.
+__host__ __device__ __forceinline__ long long ring_length(const Layout& L) {
+    const long long w = L.nx - 2 * L.r, h = L.nz - 2 * L.r - 2;
+    return 2 * w + 2 * h;
+}
+
+__device__ __forceinline__ long long ring_index(const Layout& L, long long i, long long j) {
+    const int r = L.r;
+    const long long w = L.nx - 2 * r, h = L.nz - 2 * r - 2;
+    if (i == r) return j - r;
+    if (i == L.nz - r - 1) return w + (j - r);
+    if (j == r) return 2 * w + (i - r - 1);
+    if (j == L.nx - r - 1) return 2 * w + h + (i - r - 1);
+    return -1;
+}
+
+__global__ void save_ring(const float* __restrict__ u, Layout L, float* __restrict__ ring) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int r = L.r;
+    const long long w = L.nx - 2 * r, h = L.nz - 2 * r - 2;
+    long long i, j;
+    if (t < w) { i = r; j = r + t; }
+    else if (t < 2 * w) { i = L.nz - r - 1; j = r + (t - w); }
+    else if (t < 2 * w + h) { i = r + 1 + (t - 2 * w); j = r; }
+    else if (t < 2 * w + 2 * h) { i = r + 1 + (t - 2 * w - h); j = L.nx - r - 1; }
+    else return;
+    ring[t] = u[L.at2(i, j)];
+}
+
+// Transposed boundary operations of the edges normal to `axis`, one thread
+// per line: the after edge, then the before edge (the forward applies them
+// in the opposite order; they touch disjoint points). `nu1` is the previous
+// adjoint level (zero halo), read for L nu^(m+1) at the halo points.
+__global__ void fold_phase(float* __restrict__ nu, const float* __restrict__ nu1,
+                           const float* __restrict__ C, Layout L, Weights<float> W, int axis,
+                           int before, int after) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= boundary_lines(L, axis)) return;
+    const int r = L.r;
+    const int other = axis == 0 ? 1 : 0;
+    long long idx[2];
+    idx[other] = r + t;
+    const long long step = L.stride(axis);
+    const float ih2 = W.ih2[axis];
+    for (int edge = 1; edge >= 0; edge--) {
+        const int type = edge ? after : before;
+        if (type == 0) continue;
+        idx[axis] = edge ? L.extent(axis) - r - 1 : r;
+        const long long first = L.at2(idx[0], idx[1]);
+        if (type == 1) {
+            nu[first] = 0.0f;
+            continue;
+        }
+        // Neumann: halo a = first + dir q step mirrors b = first - dir q step
+        const long long inward = edge ? -step : step;
+        for (int q = 1; q <= r; q++) {
+            float lam = 0.0f;
+            for (int k = q; k <= r; k++) lam += W.c2[k] * nu1[first + (k - q) * inward];
+            const long long b = first + q * inward;
+            nu[b] += C[b] * (lam * ih2);
+        }
+    }
+}
+
+// Receiver transposes, gathered per grid point in receiver order (no
+// atomics, so the sum order is fixed): nu[p] += C[p] * sum_e wt[e] g[rec[e]].
+__global__ void adjoint_receivers(float* __restrict__ nu, const float* __restrict__ C,
+                                  const long long* __restrict__ pts,
+                                  const int* __restrict__ rowptr, const int* __restrict__ rec,
+                                  const float* __restrict__ wt,
+                                  const float* __restrict__ g_row, int npts) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npts) return;
+    float s = 0.0f;
+    for (int e = rowptr[t]; e < rowptr[t + 1]; e++) s += wt[e] * g_row[rec[e]];
+    const long long p = pts[t];
+    nu[p] += C[p] * s;
+}
+
+// grad += nu^m K (w^m - 2 u^(m-1) + u^(m-2)) over the interior; w^m comes
+// from the saved ring where `ring` is set.
+__global__ void accumulate_gradient(float* __restrict__ grad, const float* __restrict__ nu,
+                                    const float* __restrict__ u_m,
+                                    const float* __restrict__ u_m1,
+                                    const float* __restrict__ u_m2,
+                                    const float* __restrict__ K,
+                                    const float* __restrict__ ring, Layout L) {
+    const int r = L.r;
+    const long long j = r + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long i = r + blockIdx.y * (long long)blockDim.y + threadIdx.y;
+    if (j >= L.nx - r || i >= L.nz - r) return;
+    const long long p = L.at2(i, j);
+    float w = u_m[p];
+    if (ring) {
+        const long long ri = ring_index(L, i, j);
+        if (ri >= 0) w = ring[ri];
+    }
+    const float d2 = (w - 2.0f * u_m1[p]) + u_m2[p];
+    grad[p] += nu[p] * K[p] * d2;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct Scratch {
+    cudaStream_t st;
+    std::vector<void*> blocks;
+    explicit Scratch(cudaStream_t s) : st(s) {}
+    template <typename T>
+    T* get(size_t count) {
+        void* p = nullptr;
+        GR_CUDA(cudaMallocAsync(&p, std::max<size_t>(count, 1) * sizeof(T), st));
+        blocks.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~Scratch() {
+        for (void* p : blocks) cudaFreeAsync(p, st);
+    }
+};
+
+struct Ctx {
+    Layout L;
+    Weights<float> W;
+    float dt;
+    const float* vel;
+    const float* damp;
+    const float* wavelet;
+    size_t wavelet_count;
+    Windows<float> src, rec;
+    int bc[4];
+    size_t begin, end;
+    float* C = nullptr;
+    float* Q = nullptr;
+    int zero_box[6] = {0, 0, 0, 0, 0, 0};
+    bool tiled = false;
+    long long grid = 0;  // elements of one grid (nz * pitch)
+    bool dirichlet = false;
+};
+
+// Checks the problem and copies the windows to the host (`src_iv`, ...).
+struct HostWindows {
+    std::vector<size_t> iv, off;
+    std::vector<float> val;
+};
+
+static void fetch_windows(const size_t* div, const float* dval, const size_t* doff,
+                          size_t val_size, size_t count, HostWindows& H, cudaStream_t st) {
+    H.iv.assign(count * 4, 0);
+    H.off.assign(count + 1, 0);
+    H.val.assign(val_size, 0.0f);
+    if (!count) return;
+    GR_CUDA(cudaMemcpyAsync(H.iv.data(), div, H.iv.size() * sizeof(size_t),
+                            cudaMemcpyDeviceToHost, st));
+    GR_CUDA(cudaMemcpyAsync(H.off.data(), doff, count * sizeof(size_t),
+                            cudaMemcpyDeviceToHost, st));
+    if (val_size)
+        GR_CUDA(cudaMemcpyAsync(H.val.data(), dval, val_size * sizeof(float),
+                                cudaMemcpyDeviceToHost, st));
+    GR_CUDA(cudaStreamSynchronize(st));
+}
+
+static void check_interior_windows(const char* what, const HostWindows& H, size_t count,
+                                   const Layout& L) {
+    for (size_t s = 0; s < count; s++) {
+        const size_t* b = &H.iv[s * 4];
+        const long long ext[2] = {L.nz, L.nx};
+        for (int a = 0; a < 2; a++) {
+            if (b[2 * a] > b[2 * a + 1] || (long long)b[2 * a] < L.r ||
+                (long long)b[2 * a + 1] > ext[a] - L.r - 1)
+                refuse(SIMWAVE_E_ARGUMENT,
+                       std::string(what) + " window " + std::to_string(s) +
+                           " reaches the halo or is empty (the gradient needs "
+                           "windows inside the interior)");
+        }
+        const size_t len = (b[1] - b[0] + 1) + (b[3] - b[2] + 1);
+        if (H.off[s] + len > H.val.size())
+            refuse(SIMWAVE_E_ARGUMENT, std::string(what) + " values offsets out of range");
+    }
+}
+
+static Ctx make_ctx(const simwave_problem* P, cudaStream_t st, HostWindows* rec_out) {
+    if (!P) refuse(SIMWAVE_E_ARGUMENT, "null problem");
+    if (P->dim != 2 || P->variable_density || P->precision != 4)
+        refuse(SIMWAVE_E_ARGUMENT,
+               "the gradient supports 2D float32 constant-density problems");
+    if (P->space_order < 2 || P->space_order > 2 * kMaxRadius || P->space_order % 2)
+        refuse(SIMWAVE_E_ARGUMENT, "space_order must be even, 2..20");
+    if (!P->velocity || !P->damp || !P->coeff_order2 || !P->boundary_conditions ||
+        (P->num_sources && (!P->wavelet || !P->src_points_interval ||
+                            !P->src_points_values || !P->src_points_values_offset)) ||
+        (P->num_receivers && (!P->receivers || !P->rec_points_interval ||
+                              !P->rec_points_values || !P->rec_points_values_offset)))
+        refuse(SIMWAVE_E_ARGUMENT, "null array argument");
+    if (P->begin_timestep < 1 || P->end_timestep < P->begin_timestep)
+        refuse(SIMWAVE_E_ARGUMENT, "need 1 <= begin_timestep <= end_timestep");
+    if (P->num_sources && P->wavelet_size < P->end_timestep)
+        refuse(SIMWAVE_E_ARGUMENT, "wavelet shorter than end_timestep");
+    if (P->num_sources && P->wavelet_count != 1 && P->wavelet_count != P->num_sources)
+        refuse(SIMWAVE_E_ARGUMENT, "wavelet_count must be 1 or num_sources");
+    Ctx X;
+    const int r = P->space_order / 2;
+    X.L.dim = 2;
+    X.L.r = r;
+    X.L.nz = (long long)P->nz;
+    X.L.nx = (long long)P->nx;
+    X.L.ny = 1;
+    X.L.pitch = (long long)P->pitch;
+    X.L.lead = (long long)P->lead;
+    X.L.plane = X.L.pitch;
+    X.L.slot = X.L.nz * X.L.pitch;
+    X.grid = X.L.slot;
+    if (P->pitch < P->lead + P->nx) refuse(SIMWAVE_E_ARGUMENT, "pitch < lead + nx");
+    // interior lines of opposite edges must not overlap (Neumann mirrors)
+    if (X.L.nz - 2 * r < 2 * r + 2 || X.L.nx - 2 * r < 2 * r + 2)
+        refuse(SIMWAVE_E_ARGUMENT, "grid too small for the space order");
+    for (int e = 0; e < 4; e++) {
+        if (P->boundary_conditions[e] > 2)
+            refuse(SIMWAVE_E_ARGUMENT, "boundary code must be 0, 1 or 2");
+        X.bc[e] = (int)P->boundary_conditions[e];
+        X.dirichlet |= X.bc[e] == 1;
+    }
+    HostWindows S;
+    fetch_windows(P->src_points_interval, (const float*)P->src_points_values,
+                  P->src_points_values_offset, P->src_points_values_size, P->num_sources, S,
+                  st);
+    check_interior_windows("source", S, P->num_sources, X.L);
+    HostWindows R;
+    fetch_windows(P->rec_points_interval, (const float*)P->rec_points_values,
+                  P->rec_points_values_offset, P->rec_points_values_size, P->num_receivers,
+                  R, st);
+    check_interior_windows("receiver", R, P->num_receivers, X.L);
+    if (rec_out) *rec_out = std::move(R);
+    X.W = make_weights<float>((const float*)P->coeff_order2, nullptr, r, P->dz, P->dx, 1.0);
+    X.dt = (float)P->dt;
+    X.vel = (const float*)P->velocity;
+    X.damp = (const float*)P->damp;
+    X.wavelet = (const float*)P->wavelet;
+    X.wavelet_count = P->wavelet_count;
+    X.src = Windows<float>{P->src_points_interval, (const float*)P->src_points_values,
+                           P->src_points_values_offset, P->num_sources};
+    X.rec = Windows<float>{P->rec_points_interval, (const float*)P->rec_points_values,
+                           P->rec_points_values_offset, P->num_receivers};
+    X.begin = P->begin_timestep;
+    X.end = P->end_timestep;
+    return X;
+}
+
+// Per-point coefficients C, Q of the forward stencil and the damping-free box.
+static void prepare_coefficients(Ctx& X, Scratch& mem, bool aligned) {
+    X.C = mem.get<float>((size_t)X.grid);
+    X.Q = mem.get<float>((size_t)X.grid);
+    form_coefficients(X.vel, X.damp, X.C, X.Q, X.grid, X.dt, mem.st);
+    GR_LAUNCHED("form_coefficients");
+    X.tiled = aligned && tiled2d_supported(X.L);
+    if (!X.tiled) return;
+    int* words = mem.get<int>(16);
+    find_zero_box(X.Q, X.L, words, mem.st);
+    GR_LAUNCHED("find_zero_box");
+    int box[7];
+    GR_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, mem.st));
+    GR_CUDA(cudaStreamSynchronize(mem.st));
+    const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
+    for (int i = 0; i < 6; i++) X.zero_box[i] = good ? box[i] : 0;
+}
+
+// The forward stencil on (un, uc, up): the tiled kernel on C and Q, else the
+// one-thread-per-point kernel.
+static void stencil(const Ctx& X, float* un, const float* uc, const float* up,
+                    cudaStream_t st) {
+    if (X.tiled) {
+        tiled2d_launch(X.L, false, un, uc, up, X.C, X.Q, nullptr, X.W, X.zero_box, st);
+        GR_LAUNCHED("stencil2d_single");
+        return;
+    }
+    const int r = X.L.r;
+    dim3 block(32, 8, 1);
+    dim3 grid((unsigned)((X.L.nx - 2 * r + 31) / 32), (unsigned)((X.L.nz - 2 * r + 7) / 8), 1);
+    stencil_generic<float, 2, false><<<grid, block, 0, st>>>(
+        un, uc, up, X.vel, nullptr, X.damp, X.L, X.W, X.dt, X.dt * X.dt);
+    GR_LAUNCHED("stencil_generic");
+}
+
+// One forward step n: u^(n+1) into un from uc = u^n, up = u^(n-1); the
+// values of the Dirichlet lines before the boundary conditions into
+// `ring_row`, the record of u^n into `rec_row` (either may be null).
+static void forward_step(const Ctx& X, float* un, const float* uc, const float* up,
+                         size_t n, float* ring_row, float* rec_row, cudaStream_t st) {
+    stencil(X, un, uc, up, st);
+    if (X.src.count) {
+        inject_sources<float, 2><<<(unsigned)X.src.count, 128, 0, st>>>(
+            un, X.vel, X.damp, X.L, X.src, X.wavelet, X.wavelet_count, n, X.dt,
+            X.dt * X.dt);
+        GR_LAUNCHED("inject_sources");
+    }
+    if (ring_row) {
+        const long long len = ring_length(X.L);
+        save_ring<<<(unsigned)((len + 255) / 256), 256, 0, st>>>(un, X.L, ring_row);
+        GR_LAUNCHED("save_ring");
+    }
+    const int phases[2] = {1, 0};  // x edges, then z edges
+    for (int a : phases) {
+        const int b0 = X.bc[2 * a], b1 = X.bc[2 * a + 1];
+        if (!b0 && !b1) continue;
+        const long long lines = boundary_lines(X.L, a);
+        boundary_phase<float><<<(unsigned)((lines + 255) / 256), 256, 0, st>>>(un, X.L, a,
+                                                                               b0, b1);
+        GR_LAUNCHED("boundary_phase");
+    }
+    if (rec_row && X.rec.count) {
+        const size_t threads = X.rec.count * 32;
+        record_receivers<float, 2><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+            rec_row, uc, X.L, X.rec);
+        GR_LAUNCHED("record_receivers");
+    }
+}
+
+static size_t checkpoint_count(size_t steps, size_t interval) {
+    return (steps + interval - 1) / interval;
+}
+
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+static void forward_pass(const simwave_problem* P, size_t interval, float* ck,
+                         cudaStream_t st) {
+    if (interval < 1) refuse(SIMWAVE_E_ARGUMENT, "interval must be >= 1");
+    if (!ck) refuse(SIMWAVE_E_ARGUMENT, "null checkpoint buffer");
+    Ctx X = make_ctx(P, st, nullptr);
+    Scratch mem(st);
+    float* lev = mem.get<float>(3 * (size_t)X.grid);
+    GR_CUDA(cudaMemsetAsync(lev, 0, 3 * (size_t)X.grid * sizeof(float), st));
+    prepare_coefficients(X, mem, aligned16(lev));
+    const size_t bytes = (size_t)X.grid * sizeof(float);
+    float* rec = (float*)P->receivers;
+    for (size_t n = X.begin; n <= X.end; n++) {
+        float* un = lev + ((n + 1) % 3) * X.grid;
+        const float* uc = lev + (n % 3) * X.grid;
+        const float* up = lev + ((n + 2) % 3) * X.grid;  // (n - 1) mod 3
+        const size_t i = n - X.begin;
+        if (i % interval == 0) {
+            float* dst = ck + 2 * (i / interval) * X.grid;
+            GR_CUDA(cudaMemcpyAsync(dst, up, bytes, cudaMemcpyDeviceToDevice, st));
+            GR_CUDA(cudaMemcpyAsync(dst + X.grid, uc, bytes, cudaMemcpyDeviceToDevice, st));
+        }
+        forward_step(X, un, uc, up, n, nullptr, rec ? rec + (n - 1) * X.rec.count : nullptr,
+                     st);
+    }
+}
+
+// Receiver transposes as a point-major table (receiver order within a point).
+struct AdjointTable {
+    long long* pts = nullptr;
+    int* rowptr = nullptr;
+    int* rec = nullptr;
+    float* wt = nullptr;
+    int npts = 0;
+};
+
+static AdjointTable build_table(const HostWindows& H, size_t count, const Layout& L,
+                                Scratch& mem) {
+    struct Entry {
+        long long p;
+        int s;
+        float w;
+    };
+    std::vector<Entry> e;
+    for (size_t s = 0; s < count; s++) {
+        const size_t* b = &H.iv[s * 4];
+        const size_t lz = b[1] - b[0] + 1, lx = b[3] - b[2] + 1;
+        const float* kz = H.val.data() + H.off[s];
+        const float* kx = kz + lz;
+        for (size_t iz = 0; iz < lz; iz++)
+            for (size_t ix = 0; ix < lx; ix++)
+                e.push_back({L.at2((long long)(b[0] + iz), (long long)(b[2] + ix)), (int)s,
+                             kz[iz] * kx[ix]});
+    }
+    std::stable_sort(e.begin(), e.end(), [](const Entry& a, const Entry& b) { return a.p < b.p; });
+    std::vector<long long> pts;
+    std::vector<int> rowptr{0}, rec;
+    std::vector<float> wt;
+    for (size_t k = 0; k < e.size(); k++) {
+        if (k == 0 || e[k].p != e[k - 1].p) {
+            if (k) rowptr.push_back((int)rec.size());
+            pts.push_back(e[k].p);
+        }
+        rec.push_back(e[k].s);
+        wt.push_back(e[k].w);
+    }
+    if (!e.empty()) rowptr.push_back((int)rec.size());
+    AdjointTable T;
+    T.npts = (int)pts.size();
+    if (!T.npts) return T;
+    T.pts = mem.get<long long>(pts.size());
+    T.rowptr = mem.get<int>(rowptr.size());
+    T.rec = mem.get<int>(rec.size());
+    T.wt = mem.get<float>(wt.size());
+    GR_CUDA(cudaMemcpyAsync(T.pts, pts.data(), pts.size() * sizeof(long long),
+                            cudaMemcpyHostToDevice, mem.st));
+    GR_CUDA(cudaMemcpyAsync(T.rowptr, rowptr.data(), rowptr.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, mem.st));
+    GR_CUDA(cudaMemcpyAsync(T.rec, rec.data(), rec.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, mem.st));
+    GR_CUDA(cudaMemcpyAsync(T.wt, wt.data(), wt.size() * sizeof(float),
+                            cudaMemcpyHostToDevice, mem.st));
+    // the host vectors die at return: wait for the copies
+    GR_CUDA(cudaStreamSynchronize(mem.st));
+    return T;
+}
+
+static void reverse_pass(const simwave_problem* P, size_t interval, const float* ck,
+                         const float* g, float* grad, cudaStream_t st) {
+    if (interval < 1) refuse(SIMWAVE_E_ARGUMENT, "interval must be >= 1");
+    if (!ck || !grad || (P && P->num_receivers && !g))
+        refuse(SIMWAVE_E_ARGUMENT, "null checkpoint, cotangent or gradient buffer");
+    HostWindows R;
+    Ctx X = make_ctx(P, st, &R);
+    Scratch mem(st);
+    const size_t G = (size_t)X.grid, bytes = G * sizeof(float);
+    const size_t steps = X.end - X.begin + 1;
+    const size_t K = std::min(interval, steps);
+    float* seg = mem.get<float>((K + 2) * G);
+    float* nu = mem.get<float>(3 * G);
+    float* Kf = mem.get<float>(G);
+    const long long ring_len = ring_length(X.L);
+    float* ring = X.dirichlet ? mem.get<float>(K * (size_t)ring_len) : nullptr;
+    GR_CUDA(cudaMemsetAsync(seg, 0, (K + 2) * bytes, st));
+    GR_CUDA(cudaMemsetAsync(nu, 0, 3 * bytes, st));
+    GR_CUDA(cudaMemsetAsync(grad, 0, bytes, st));
+    prepare_coefficients(X, mem, aligned16(seg) && aligned16(nu));
+    gradient_factor<<<1024, 256, 0, st>>>(X.vel, Kf, (long long)G, X.dt);
+    GR_LAUNCHED("gradient_factor");
+    const AdjointTable T = build_table(R, P->num_receivers, X.L, mem);
+
+    const int r = X.L.r;
+    const dim3 gblock(32, 8, 1);
+    const dim3 ggrid((unsigned)((X.L.nx - 2 * r + 31) / 32),
+                     (unsigned)((X.L.nz - 2 * r + 7) / 8), 1);
+    const size_t b = X.begin, e = X.end;
+    const size_t nck = checkpoint_count(steps, interval);
+    for (size_t j = nck; j-- > 0;) {
+        const size_t n0 = b + j * interval;
+        const size_t n1 = std::min(n0 + interval - 1, e);
+        // levels u^(n0-1) .. u^(n1+1) at seg[k - (n0 - 1)]
+        GR_CUDA(cudaMemcpyAsync(seg, ck + 2 * j * G, 2 * bytes, cudaMemcpyDeviceToDevice, st));
+        for (size_t n = n0; n <= n1; n++) {
+            const size_t k = n - n0;
+            forward_step(X, seg + (k + 2) * G, seg + (k + 1) * G, seg + k * G, n,
+                         ring ? ring + k * (size_t)ring_len : nullptr, nullptr, st);
+        }
+        for (size_t m = n1 + 1; m >= n0 + 1; m--) {
+            if (m == e + 1) continue;  // nu^(e+1) = 0: no record reads u^(e+1)
+            float* num = nu + (m % 3) * G;
+            const float* nu1 = nu + ((m + 1) % 3) * G;
+            const float* nu2 = nu + ((m + 2) % 3) * G;
+            stencil(X, num, nu1, nu2, st);
+            if (T.npts) {
+                adjoint_receivers<<<(unsigned)((T.npts + 255) / 256), 256, 0, st>>>(
+                    num, X.C, T.pts, T.rowptr, T.rec, T.wt, g + (m - 1) * P->num_receivers,
+                    T.npts);
+                GR_LAUNCHED("adjoint_receivers");
+            }
+            const int phases[2] = {0, 1};  // transposed order: z edges, then x edges
+            for (int a : phases) {
+                const int b0 = X.bc[2 * a], b1 = X.bc[2 * a + 1];
+                if (!b0 && !b1) continue;
+                const long long lines = boundary_lines(X.L, a);
+                fold_phase<<<(unsigned)((lines + 127) / 128), 128, 0, st>>>(
+                    num, nu1, X.C, X.L, X.W, a, b0, b1);
+                GR_LAUNCHED("fold_phase");
+            }
+            const size_t k = m - n0;  // seg index of u^(m-1); u^m at k + 1
+            accumulate_gradient<<<ggrid, gblock, 0, st>>>(
+                grad, num, seg + (k + 1) * G, seg + k * G, seg + (k - 1) * G, Kf,
+                ring ? ring + (m - 1 - n0) * (size_t)ring_len : nullptr, X.L);
+            GR_LAUNCHED("accumulate_gradient");
+        }
+    }
+}
+
+template <typename F>
+static int guarded(F&& f) {
+    try {
+        f();
+        return SIMWAVE_OK;
+    } catch (const Refusal& r) {
+        ::sw::record_error(r.message);
+        return r.code;
+    } catch (const std::exception& ex) {
+        ::sw::record_error(ex.what());
+        return SIMWAVE_E_CUDA;
+    }
+}
+
+}  // namespace grad
+}  // namespace sw
+
+extern "C" int simwave_gradient_checkpoints(const simwave_problem* problem, size_t interval,
+                                            size_t* grids) {
+    return sw::grad::guarded([&] {
+        if (!problem || !grids || interval < 1 ||
+            problem->end_timestep < problem->begin_timestep)
+            sw::grad::refuse(SIMWAVE_E_ARGUMENT, "invalid checkpoint request");
+        const size_t steps = problem->end_timestep - problem->begin_timestep + 1;
+        *grids = 2 * sw::grad::checkpoint_count(steps, interval);
+    });
+}
+
+extern "C" int simwave_gradient_forward(const simwave_problem* problem, size_t interval,
+                                        void* checkpoints, void* stream) {
+    return sw::grad::guarded([&] {
+        sw::grad::forward_pass(problem, interval, static_cast<float*>(checkpoints),
+                               static_cast<cudaStream_t>(stream));
+    });
+}
+
+extern "C" int simwave_gradient_backward(const simwave_problem* problem, size_t interval,
+                                         const void* checkpoints, const void* grad_receivers,
+                                         void* grad_velocity, void* stream) {
+    return sw::grad::guarded([&] {
+        sw::grad::reverse_pass(problem, interval, static_cast<const float*>(checkpoints),
+                               static_cast<const float*>(grad_receivers),
+                               static_cast<float*>(grad_velocity),
+                               static_cast<cudaStream_t>(stream));
+    });
+}

@@ -248,20 +248,9 @@ static int run(const simwave_problem* P, cudaStream_t st) {
     ctx.coefQ = Q;
 
     // weights: unscaled half weights, per-axis 1/h^2 and 1/(4 h^2)
-    Weights<float> W;
-    std::memset(&W, 0, sizeof(W));
-    const float* c2 = (const float*)P->coeff_order2;
-    const float* c1 = vd ? (const float*)P->coeff_order1 : nullptr;
-    for (int k = 0; k <= r; k++) {
-        W.c2[k] = c2[k];
-        W.c1[k] = c1 ? c1[k] : 0.f;
-    }
-    const double h[3] = {P->dz, P->dx, P->dy};
-    for (int a = 0; a < 3; a++) {
-        const float h2 = (float)h[a] * (float)h[a];
-        W.ih2[a] = (float)(1.0 / (double)h2);
-        W.s1[a] = (float)(1.0 / (4.0 * (double)h2));
-    }
+    const Weights<float> W = make_weights<float>(
+        (const float*)P->coeff_order2, vd ? (const float*)P->coeff_order1 : nullptr, r,
+        P->dz, P->dx, P->dy);
     const float dt = (float)P->dt, dt2 = dt * dt;
     int bc[6];
     for (int e = 0; e < 6; e++) bc[e] = (int)P->boundary_conditions[e];

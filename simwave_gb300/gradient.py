@@ -1,0 +1,102 @@
+"""Velocity gradient of the forward loop (``simwave_gradient_*`` of the C
+library) behind ``torch.autograd``.
+
+``shot_record(velocity, problem)`` runs the forward loop of a
+``DeviceProblem`` on the given velocity grid and returns its shot record as a
+differentiable tensor; ``backward`` runs the discrete adjoint with
+checkpointed recomputation (a level pair every ``interval`` steps, ``interval``
+= ceil(sqrt(steps)) by default, so memory grows with sqrt(T) instead of T).
+2D float32 constant-density problems; the reference offers only the forward
+operator (simwave/kernel/backend/compiler.py:128-130).
+
+``misfit_gradient(velocity, problems, observed)`` is the full-waveform
+inversion step: the L2 misfit 0.5 * sum((rec - obs)^2) over shots and its
+velocity gradient.
+"""
+import ctypes
+import math
+
+import torch
+
+from .backend import _lib
+from .device import DeviceProblem
+
+
+def _check(status, what):
+    if status != 0:
+        raise RuntimeError("{} failed ({}): {}".format(what, status, _lib.last_error()))
+
+
+def default_interval(steps):
+    return max(1, int(math.ceil(math.sqrt(steps))))
+
+
+class _ShotRecord(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, velocity, problem, interval):
+        if velocity.shape != tuple(problem.shape):
+            raise ValueError("velocity shape {} != problem grid {}".format(
+                tuple(velocity.shape), tuple(problem.shape)))
+        lib = _lib.load()
+        p = problem.problem
+        problem._view(problem.vel, None).copy_(velocity.detach())
+        grids = ctypes.c_size_t()
+        _check(lib.simwave_gradient_checkpoints(ctypes.byref(p), ctypes.c_size_t(interval),
+                                                ctypes.byref(grids)), "checkpoint count")
+        ck = torch.empty(grids.value * problem.slot, dtype=torch.float32,
+                         device=problem.device)
+        stream = torch.cuda.current_stream(problem.device)
+        _check(lib.simwave_gradient_forward(ctypes.byref(p), ctypes.c_size_t(interval),
+                                            ctypes.c_void_p(ck.data_ptr()),
+                                            ctypes.c_void_p(stream.cuda_stream)),
+               "simwave_gradient_forward")
+        ctx.problem = problem
+        ctx.interval = interval
+        ctx.save_for_backward(ck)
+        return problem.receivers[:, :problem.nrec].clone()
+
+    @staticmethod
+    def backward(ctx, grad_rec):
+        (ck,) = ctx.saved_tensors
+        problem = ctx.problem
+        lib = _lib.load()
+        g = grad_rec.detach().to(torch.float32).contiguous()
+        out = torch.empty(problem.slot, dtype=torch.float32, device=problem.device)
+        stream = torch.cuda.current_stream(problem.device)
+        _check(lib.simwave_gradient_backward(
+            ctypes.byref(problem.problem), ctypes.c_size_t(ctx.interval),
+            ctypes.c_void_p(ck.data_ptr()), ctypes.c_void_p(g.data_ptr()),
+            ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
+            "simwave_gradient_backward")
+        return problem._view(out, None).contiguous(), None, None
+
+
+def shot_record(velocity, problem, interval=None):
+    """Differentiable shot record ``(end_timestep, num_receivers)`` of
+    ``problem`` (a ``DeviceProblem``) on ``velocity`` (the extended grid,
+    float32, on the problem's device)."""
+    if not isinstance(problem, DeviceProblem):
+        raise TypeError("expected a DeviceProblem")
+    if problem.dim != 2 or problem.vd or problem.dtype.itemsize != 4:
+        raise ValueError("the gradient supports 2D float32 constant-density problems")
+    steps = problem.timesteps
+    return _ShotRecord.apply(velocity, problem, int(interval or default_interval(steps)))
+
+
+def misfit_gradient(velocity, problems, observed, interval=None):
+    """L2 misfit over shots and its velocity gradient.
+
+    ``velocity``: the extended grid (float32 tensor on the device);
+    ``problems``: one ``DeviceProblem`` per shot on that grid; ``observed``:
+    one shot record per shot (tensor or array, same shape as the record).
+    Returns ``(misfit, gradient)`` with the gradient on the extended grid.
+    """
+    v = velocity.detach().clone().requires_grad_(True)
+    total = 0.0
+    for prob, obs in zip(problems, observed):
+        obs = torch.as_tensor(obs, dtype=torch.float32, device=v.device)
+        rec = shot_record(v, prob, interval)
+        loss = 0.5 * torch.sum((rec - obs) ** 2)
+        loss.backward()
+        total += float(loss.detach())
+    return total, v.grad

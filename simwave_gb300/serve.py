@@ -8,8 +8,11 @@ host when the shot completes.
 * 2D float32 shots join a running ``BatchEngine``: every epoch advances all
   admitted 2D shots by ``epoch_steps`` time steps in one graph-captured
   sequence, and newly admitted shots join at the next epoch.
-* Other shots (3D, or float64) run through the device entry on one of a few
-  CUDA streams, so their work overlaps the 2D epochs and each other.
+* Other shots (3D, or float64) run through the device entry on a
+  low-priority stream, shortest first (interior updates), at most
+  ``inflight`` queued at a time; each one fills the GPU on its own, so running
+  them side by side would only delay all of them. The 2D epochs run on a
+  high-priority stream and overlap them at block granularity.
 
 Latency of a request = completion time - arrival time (queueing, upload,
 compute and shot-record download included).
@@ -54,6 +57,7 @@ class Request:
         self.bytes = footprint_bytes(kwargs)
         v = kwargs["velocity_model"]
         self.batchable = v.ndim == 2 and v.dtype == np.float32
+        self.updates = int(np.prod(v.shape)) * int(kwargs["end_timestep"])
 
     @property
     def latency(self):
@@ -63,7 +67,7 @@ class Request:
 class ShotServer:
     """Serve requests with continuous batching on one GPU."""
 
-    def __init__(self, hbm_budget=None, epoch_steps=64, streams=4, device="cuda",
+    def __init__(self, hbm_budget=None, epoch_steps=64, inflight=2, device="cuda",
                  tile_rows=None):
         self.device = torch.device(device)
         free, _ = torch.cuda.mem_get_info(self.device)
@@ -74,11 +78,14 @@ class ShotServer:
         self.engine = BatchEngine(device)
         for order, rows in (tile_rows or {}).items():
             self.engine.set_tile_rows(order, rows)
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(max(streams, 1))]
-        self._next_stream = 0
+        lo, hi = torch.cuda.Stream.priority_range()
+        self.epoch_stream = torch.cuda.Stream(self.device, priority=hi)
+        self.shot_stream = torch.cuda.Stream(self.device, priority=lo)
+        self.inflight = max(int(inflight), 1)
         self.pending = collections.deque()
         self.active2d = {}   # shot id -> request
-        self.active = []     # (request, event) of stream-run shots
+        self.ready = []      # admitted stream-run shots not yet launched
+        self.active = []     # (request, event) of launched stream-run shots
         self.done = []
 
     # -- admission ----------------------------------------------------------
@@ -106,16 +113,24 @@ class ShotServer:
                 sid = self.engine.add(req.problem)
                 self.active2d[sid] = req
             else:
-                stream = self.streams[self._next_stream % len(self.streams)]
-                self._next_stream += 1
-                # the uploads above were queued on the current stream
-                stream.wait_stream(torch.cuda.current_stream(self.device))
-                req.problem.run(stream)
-                ev = torch.cuda.Event()
-                ev.record(stream)
-                self.active.append((req, ev))
+                self.ready.append(req)
             admitted = True
+        # the uploads above were queued on the current stream
+        if admitted:
+            self.epoch_stream.wait_stream(torch.cuda.current_stream(self.device))
+            self.shot_stream.wait_stream(torch.cuda.current_stream(self.device))
+        self._launch()
         return admitted
+
+    def _launch(self):
+        """Queue the shortest admitted stream-run shots on the shot stream."""
+        while self.ready and len(self.active) < self.inflight:
+            req = min(self.ready, key=lambda r: r.updates)
+            self.ready.remove(req)
+            req.problem.run(self.shot_stream)
+            ev = torch.cuda.Event()
+            ev.record(self.shot_stream)
+            self.active.append((req, ev))
 
     def _evict(self, need):
         for req in self.done:
@@ -143,7 +158,7 @@ class ShotServer:
     def _retire(self):
         finished = [sid for sid in self.active2d if self.engine.remaining(sid) == 0]
         if finished:
-            torch.cuda.synchronize(self.device)
+            self.epoch_stream.synchronize()
             for sid in finished:
                 self.engine.release(sid)
                 self._complete(self.active2d.pop(sid))
@@ -155,6 +170,7 @@ class ShotServer:
             else:
                 still.append((req, ev))
         self.active = still
+        self._launch()
 
     # -- loop ---------------------------------------------------------------
     def serve(self, requests, clock_start=None, timeout=600.0):
@@ -174,9 +190,9 @@ class ShotServer:
                     len(self.done), total, timeout))
             self._admit(now)
             if self.active2d:
-                self.engine.run(self.epoch_steps)
+                self.engine.run(self.epoch_steps, stream=self.epoch_stream)
                 # bound the queue ahead of the host: wait for this epoch
-                torch.cuda.current_stream(self.device).synchronize()
+                self.epoch_stream.synchronize()
             elif self.active:
                 time.sleep(0.0005)
             elif self.pending:

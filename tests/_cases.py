@@ -109,3 +109,60 @@ def random_problem(sw, dim, order, vd, bc, stride, dtype=np.float32, n=32,
     solver = sw.Solver(space_model=sm, time_model=tm, sources=source,
                        receivers=receiver, wavelet=wavelet)
     return solver.forward_arguments()
+
+
+def edge_problem(bc, order=4, shape=(22, 26), timesteps=160, seed=0,
+                 dtype=np.float64, damping=0.0, nsrc=1):
+    """Middleware kwargs of a small 2D constant-density problem whose waves
+    reach every edge many times: no damping layer (or a uniform ``damping``),
+    a source window near the centre and receiver windows on the first and
+    second interior lines of every edge (the lines the boundary conditions
+    act on). Window values are random; the wavelet is random per source."""
+    from simwave_gb300.frontend.fd import half_coefficients
+    rng = np.random.default_rng(seed)
+    nz, nx = shape
+    r = order // 2
+    vel = (1500.0 + 1000.0 * rng.random(shape)).astype(dtype)
+    h, dt = 10.0, 1.0e-3
+
+    def windows(boxes):
+        iv, vals, off = [], [], [0]
+        for z0, z1, x0, x1 in boxes:
+            iv += [z0, z1, x0, x1]
+            v = rng.uniform(0.2, 1.0, (z1 - z0 + 1) + (x1 - x0 + 1))
+            vals += list(v)
+            off.append(off[-1] + len(v))
+        return (np.array(iv, dtype=np.uint64), np.array(vals, dtype=dtype),
+                np.array(off, dtype=np.uint64))
+
+    cz, cx = nz // 2, nx // 2
+    src_boxes = [(cz - 1 + s, cz + 1 + s, cx - 1, cx + 1) for s in range(nsrc)]
+    lo_z, hi_z, lo_x, hi_x = r, nz - r - 1, r, nx - r - 1
+    rec_boxes = [(lo_z, lo_z + 1, cx - 2, cx + 1), (hi_z - 1, hi_z, cx, cx + 2),
+                 (cz - 2, cz, lo_x, lo_x + 1), (cz, cz + 2, hi_x - 1, hi_x),
+                 (lo_z, lo_z, lo_x, lo_x + 1), (hi_z, hi_z, hi_x, hi_x),
+                 (cz + 3, cz + 4, cx + 3, cx + 4)]
+    siv, sval, soff = windows(src_boxes)
+    riv, rval, roff = windows(rec_boxes)
+    w = rng.standard_normal((timesteps, nsrc)).astype(dtype)
+    nslots = 3
+    return dict(
+        u_full=np.zeros((nslots,) + shape, dtype=dtype),
+        velocity_model=vel, density_model=None,
+        damping_mask=np.full(shape, damping, dtype=dtype),
+        wavelet=w.reshape(-1) if nsrc > 1 else w[:, 0].copy(),
+        wavelet_size=timesteps, wavelet_count=nsrc,
+        second_order_fd_coefficients=np.asarray(half_coefficients(2, order), dtype=dtype),
+        first_order_fd_coefficients=np.asarray(half_coefficients(1, order), dtype=dtype),
+        boundary_condition=tuple(bc),
+        src_points_interval=siv, src_points_interval_size=len(siv),
+        src_points_values=sval, src_points_values_offset=soff,
+        src_points_values_size=len(sval),
+        rec_points_interval=riv, rec_points_interval_size=len(riv),
+        rec_points_values=rval, rec_points_values_offset=roff,
+        rec_points_values_size=len(rval),
+        shot_record=np.zeros((timesteps, len(rec_boxes)), dtype=dtype),
+        num_sources=nsrc, num_receivers=len(rec_boxes),
+        grid_spacing=(dtype(h), dtype(h)), saving_stride=0, dt=dtype(dt),
+        begin_timestep=1, end_timestep=timesteps, space_order=order,
+        num_snapshots=nslots)

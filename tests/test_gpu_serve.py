@@ -1,6 +1,6 @@
 """Continuous-batching server: every request's result is the same served in
-a mix (2D batched with other shots, 3D overlapping on streams, admission
-gated by the HBM budget) as run alone."""
+a mix (2D batched with other shots, 3D on a side stream overlapping the 2D
+epochs, admission gated by the HBM budget) as run alone."""
 import numpy as np
 import pytest
 
@@ -73,3 +73,18 @@ def test_budget_gates_admission():
     server.close()
     assert all(r.completed is not None for r in reqs)
     assert max(peak) <= budget
+
+
+def test_stream_shots_run_shortest_first():
+    """Side-stream shots admitted together complete in order of size."""
+    from simwave_gb300.serve import Request, ShotServer
+    reqs = []
+    for i, n in enumerate((40, 24, 32, 28)):
+        kw = random_problem(sw, 3, 4, False, "none", 0, shape=(n, n, n), tf=0.05,
+                            seed=70 + i, nrec=3)
+        reqs.append(Request(kw, 0.0, tag=i))
+    server = ShotServer(inflight=1)
+    server.serve(reqs, timeout=300)
+    server.close()
+    order = [r.tag for r in sorted(reqs, key=lambda r: r.completed)]
+    assert order == [r.tag for r in sorted(reqs, key=lambda r: r.updates)]
