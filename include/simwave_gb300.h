@@ -256,6 +256,10 @@ int simwave_forward_device(const simwave_problem *problem, void *stream);
 #define SIMWAVE_POLICY_VEC_2CTA_ROT 5   /* float4, register queues rotated by
                                            unrolling, 2 CTAs per SM */
 #define SIMWAVE_POLICY_VEC_1CTA_ROT 6   /* same, 1 CTA per SM */
+#define SIMWAVE_POLICY_VEC_PACKED 7     /* float4 along y with packed f32x2
+                                           arithmetic, density z-queue in shared
+                                           memory, 2 CTAs per SM */
+#define SIMWAVE_POLICY_VEC_PACKED_1CTA 8 /* same, 1 CTA per SM */
 int simwave_set_kernel_policy(int policy);
 
 /* How the host-pointer entries move grids (process-wide).

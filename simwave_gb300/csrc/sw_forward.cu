@@ -304,14 +304,22 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         }
         ctx.ok = false;
         const size_t n = (size_t)(L.dim == 3 ? L.nz * L.plane : L.nz * L.pitch);
+        const bool gz = L.dim == 3 && wants_density_z(L, R.vd);
         void* scratch = nullptr;
-        SW_CUDA(cudaMallocAsync(&scratch, 2 * n * sizeof(float) + 16 * sizeof(int), st));
+        SW_CUDA(cudaMallocAsync(&scratch, (gz ? 3 : 2) * n * sizeof(float) + 16 * sizeof(int),
+                                st));
         ctx.scratch = scratch;
         float* C = static_cast<float*>(scratch);
         float* Q = C + n;
-        int* words = reinterpret_cast<int*>(Q + n);
+        float* G = gz ? Q + n : nullptr;
+        int* words = reinterpret_cast<int*>(Q + (gz ? 2 : 1) * n);
         form_coefficients(R.vel, R.damp, C, Q, (long long)n, (float)R.dt, st);
         SW_LAUNCHED("form_coefficients");
+        if (G) {
+            form_density_z(R.den, G, L, R.W, st);
+            SW_LAUNCHED("form_density_z");
+            ctx.coefGz = G;
+        }
         find_zero_box(Q, L, words, st);
         SW_LAUNCHED("find_zero_box");
         int box[7];
@@ -1077,7 +1085,7 @@ extern "C" int simwave_device_status(void* stream) {
 }
 
 extern "C" int simwave_set_kernel_policy(int policy) {
-    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_1CTA_ROT)
+    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_PACKED_1CTA)
         return SIMWAVE_E_ARGUMENT;
     sw::set_kernel_policy(policy);
     return SIMWAVE_OK;

@@ -126,6 +126,24 @@ __global__ void form_coefficients(const float* __restrict__ vel,
     }
 }
 
+// gz = s1_z * sum_k c1_k (rho(z+k) - rho(z-k)) over the interior (3D): the
+// density's z term of the variable-density cross term, time-invariant.
+__global__ void form_density_z(const float* __restrict__ den, float* __restrict__ gz, Layout L,
+                               Weights<float> W) {
+    const int r = L.r;
+    const long long ny = L.ny - 2 * r, nx = L.nx - 2 * r, nz = L.nz - 2 * r;
+    const long long total = nz * nx * ny;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long k = r + t % ny, j = r + (t / ny) % nx, i = r + t / (ny * nx);
+        const long long p = L.at3(i, j, k);
+        float f = W.c1[1] * (den[p + L.plane] - den[p - L.plane]);
+        for (int q = 2; q <= r; q++)
+            f = fmaf(W.c1[q], den[p + q * L.plane] - den[p - q * L.plane], f);
+        gz[p] = f * W.s1[0];
+    }
+}
+
 // u_next from the spatial operator, C, Q, u_cur and u_prev.
 __device__ __forceinline__ float leapfrog_cq(float lap, float c, float q, float ucur,
                                              float uprev) {
@@ -643,6 +661,423 @@ stencil3d_vec4(const __grid_constant__ CUtensorMap map_u,
     }
 }
 
+// ---- packed-pair arithmetic (.f32x2, sm_100 and later) -----------------------
+//
+// Two consecutive y points share one 64-bit register pair; add, sub, mul and
+// fma on .f32x2 round each half exactly like the scalar instruction, so a
+// kernel written on pairs computes what the float4 kernel computes with half
+// the arithmetic instructions. Weights are passed pre-duplicated ({w, w}).
+
+struct P2 {
+    unsigned long long v;
+};
+struct V4 {  // points y0, y0+1 (lo) and y0+2, y0+3 (hi)
+    P2 lo, hi;
+};
+
+__device__ __forceinline__ P2 pk(float a, float b) {
+    P2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpk(P2 p, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(p.v));
+}
+__device__ __forceinline__ P2 add2(P2 a, P2 b) {
+    P2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ P2 sub2(P2 a, P2 b) {
+    P2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ P2 mul2(P2 a, P2 b) {
+    P2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
+    P2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+__device__ __forceinline__ V4 vadd(V4 a, V4 b) { return {add2(a.lo, b.lo), add2(a.hi, b.hi)}; }
+__device__ __forceinline__ V4 vsub(V4 a, V4 b) { return {sub2(a.lo, b.lo), sub2(a.hi, b.hi)}; }
+__device__ __forceinline__ V4 vmul(P2 w, V4 a) { return {mul2(w, a.lo), mul2(w, a.hi)}; }
+__device__ __forceinline__ V4 vfma(P2 w, V4 a, V4 c) {
+    return {fma2(w, a.lo, c.lo), fma2(w, a.hi, c.hi)};
+}
+__device__ __forceinline__ V4 vzero() { return {{0ull}, {0ull}}; }
+
+// 16-byte loads and stores of 4 consecutive points as two pairs
+__device__ __forceinline__ V4 ldg_v4(const float* p, bool any) {
+    if (!any) return vzero();
+    const ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2*>(p));
+    return {{t.x}, {t.y}};
+}
+__device__ __forceinline__ V4 ld_v4(const float* p, bool any) {
+    if (!any) return vzero();
+    const ulonglong2 t = *reinterpret_cast<const ulonglong2*>(p);
+    return {{t.x}, {t.y}};
+}
+__device__ __forceinline__ V4 lds_v4(const void* p) {
+    V4 r;
+    asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];"
+                 : "=l"(r.lo.v), "=l"(r.hi.v)
+                 : "r"(smem_addr(p))
+                 : "memory");
+    return r;
+}
+__device__ __forceinline__ void sts_v4(void* p, V4 v) {
+    asm volatile("st.shared.v2.b64 [%0], {%1, %2};" ::"r"(smem_addr(p)), "l"(v.lo.v),
+                 "l"(v.hi.v)
+                 : "memory");
+}
+__device__ __forceinline__ float4 to_f4(V4 v) {
+    float4 r;
+    unpk(v.lo, r.x, r.y);
+    unpk(v.hi, r.z, r.w);
+    return r;
+}
+__device__ __forceinline__ V4 from_f4(float4 f) { return {pk(f.x, f.y), pk(f.z, f.w)}; }
+
+// The y window of a thread (4 * NC values from the tile row) as 64-bit
+// pairs: ev[j] = (w[2j], w[2j+1]) straight from the 16-byte loads, od[j] =
+// (w[2j+1], w[2j+2]) repacked. at(s) is the pair starting at offset s.
+template <int NC>
+struct YWindow {
+    __device__ __forceinline__ static void load(const float* t, P2* ev, P2* od) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const V4 q = lds_v4(t + 4 * c);
+            ev[2 * c] = q.lo;
+            ev[2 * c + 1] = q.hi;
+        }
+#pragma unroll
+        for (int j = 0; j < 2 * NC - 1; j++) {
+            float a, b, c, d;
+            unpk(ev[j], a, b);
+            unpk(ev[j + 1], c, d);
+            od[j] = pk(b, c);
+        }
+    }
+    __device__ __forceinline__ static P2 at(const P2* ev, const P2* od, int s) {
+        return (s & 1) ? od[s >> 1] : ev[s >> 1];
+    }
+};
+
+// Approximate reciprocal (the value __fdividef(1, x) uses, without its
+// range test); for the density and 1 + q, both far from the range limits.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Weights duplicated into pairs (kernel parameters).
+struct PairWeights {
+    unsigned long long c2[kMaxRadius + 1], c1[kMaxRadius + 1], ih2[3], s1[3], one;
+};
+
+PairWeights pair_weights(const Weights<float>& W) {
+    auto dup = [](float w) {
+        unsigned u;
+        std::memcpy(&u, &w, 4);
+        return ((unsigned long long)u << 32) | u;
+    };
+    PairWeights P;
+    for (int k = 0; k <= kMaxRadius; k++) {
+        P.c2[k] = dup(W.c2[k]);
+        P.c1[k] = dup(W.c1[k]);
+    }
+    for (int a = 0; a < 3; a++) {
+        P.ih2[a] = dup(W.ih2[a]);
+        P.s1[a] = dup(W.s1[a]);
+    }
+    P.one = dup(1.0f);
+    return P;
+}
+
+// The float4 kernel's plane loop on pairs: z, x and y derivatives, the
+// combine and the update on .f32x2. The plane loop is unrolled by the queue
+// length (static queue slots). Variable density takes the density's z term
+// either from a z-queue in shared memory (GZ false) or, with GZ, from the
+// per-point array gz = s1_z * sum_k c1_k (rho(z+k) - rho(z-k)) formed once
+// per run (form_density_z): 4 more bytes per point from memory, in exchange
+// for the queue's shared-memory traffic (9 loads and a store per plane).
+template <int R, bool VD, int MINB, bool GZ>
+__global__ void __launch_bounds__(kThreads, MINB)
+stencil3d_vec4p(const __grid_constant__ CUtensorMap map_u,
+                const __grid_constant__ CUtensorMap map_rho, float* un,
+                const float* __restrict__ uc, const float* up,
+                const float* __restrict__ coefC, const float* __restrict__ den,
+                const float* __restrict__ coefQ, const float* __restrict__ gz,
+                Layout L, Weights<float> Wt, PairWeights PW, int slot_cur, int zchunk,
+                ZeroBox zb, int* __restrict__ err) {
+    using VT = VecTile<R>;
+    constexpr int HY = VT::HY, TW = VT::TW, NC = VT::NC;
+    constexpr int NF = VD ? 2 : 1;
+    constexpr int QN = 2 * R + 1;
+    constexpr bool SQ = VD && !GZ;  // density z-queue in shared memory
+    static_assert(!GZ || VD, "gz is a variable-density term");
+    float* tiles = reinterpret_cast<float*>(sw_dyn_smem);
+    float4* sq_base = reinterpret_cast<float4*>(tiles + NF * kStages * VT::STRIDE);
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(sq_base + (SQ ? QN * kThreads : 0));
+    int& s_abort = *reinterpret_cast<int*>(bars + kStages);
+    if (*(volatile int*)err) return;
+    if (smem_addr(tiles) & 127) {
+        if (threadIdx.x == 0) atomicExch(err, SIMWAVE_E_ARGUMENT);
+        return;
+    }
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int yb = R + blockIdx.x * 128;
+    const int y0 = yb + 4 * lane;
+    const int x = R + blockIdx.y * kWarps + warp;
+    const int zbeg = R + blockIdx.z * zchunk;
+    const int zend = min(zbeg + zchunk, (int)L.nz - R);
+    if (zbeg >= zend) return;
+    const int ylim = (int)L.ny - R;
+    const bool any = x < (int)L.nx - R && y0 < ylim;
+    const bool full = any && y0 + 3 < ylim;
+    const int off = x * (int)L.pitch + (int)L.lead + y0;
+    // threads past the interior load from the last interior row / chunk
+    // (always inside the grid) instead of selecting zeros; only their
+    // stores are masked
+    const int xl = min(x, (int)L.nx - R - 1);
+    const int yl = min(y0, R + 4 * ((ylim - 1 - R) / 4));
+    const int offl = xl * (int)L.pitch + (int)L.lead + yl;
+    const int col0 = (int)L.lead + yb - HY;
+    const int row0 = blockIdx.y * kWarps;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    __syncthreads();
+    auto issue = [&](int plane, int stage) {
+        mbar_expect_tx(&bars[stage], NF * VT::BYTES);
+        tma_load_4d(tiles + stage * VT::STRIDE, &map_u, &bars[stage], col0, row0, plane,
+                    slot_cur);
+        if (VD)
+            tma_load_4d(tiles + (kStages + stage) * VT::STRIDE, &map_rho, &bars[stage], col0,
+                        row0, plane, 0);
+    };
+    int issued = 0;
+    if (threadIdx.x == 0)
+        for (; issued < kStages && zbeg + issued < zend; issued++) issue(zbeg + issued, issued);
+
+    // weight pairs held in registers for the whole chunk
+    P2 w2[R + 1], w1[R + 1];
+#pragma unroll
+    for (int k = 0; k <= R; k++) {
+        w2[k].v = PW.c2[k];
+        w1[k].v = PW.c1[k];
+    }
+    auto vs = [&](int k, V4 x, V4 acc) -> V4 { return vfma(w2[k], x, acc); };
+    auto vw = [&](bool first, int k, V4 x, V4 acc) -> V4 {
+        return first ? vmul(w1[k], x) : vfma(w1[k], x, acc);
+    };
+    auto vs0 = [&](V4 x) -> V4 { return vmul(w2[0], x); };
+
+    // queues hold planes z-R .. z+R; slot of plane p = (p - zbeg + R) mod QN
+    V4 qu[QN];
+    float4* sq = sq_base + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < QN; j++) {
+        const long long pz = (long long)(zbeg - R + j) * L.plane + offl;
+        qu[j] = ldg_v4(uc + pz, true);
+        if (SQ) sts_v4(sq + j * kThreads, ldg_v4(den + pz, true));
+    }
+    const bool xybox = x >= zb.x0 && x < zb.x1 && y0 >= zb.y0 && y0 + 3 < zb.y1;
+    // per-point operands of the next plane, fetched a plane ahead
+    V4 nprev, ncoef, nq, ngz = vzero();
+    bool nbox;
+    auto fetch = [&](int zz) {
+        const long long p = (long long)zz * L.plane + offl;
+        nprev = ld_v4(up + p, true);
+        ncoef = ldg_v4(coefC + p, true);
+        if (GZ) ngz = ldg_v4(gz + p, true);
+        nbox = xybox && zz >= zb.z0 && zz < zb.z1;
+        nq = ldg_v4(coefQ + p, !nbox);
+    };
+    fetch(zbeg);
+    int aborted_at = -1;
+    long long zoff = (long long)zbeg * L.plane;  // z * plane of the current plane
+
+    // plane z = zbeg + QN m + J: with QN a multiple of the stage count the
+    // stage and the barrier parity are compile-time functions of J
+    auto plane_step = [&](const int z, const int J, const int m) -> bool {
+        constexpr bool kStatic = QN % kStages == 0;
+        const int it = QN * m + J;
+        const int stage = kStatic ? J % kStages : it % kStages;
+        const unsigned parity =
+            kStatic ? (unsigned)(((QN / kStages) * m + J / kStages) & 1) : (unsigned)((it / kStages) & 1);
+        auto slot = [&](int d) { return (J + R + d) % QN; };  // plane z + d
+        const V4 vprev = nprev, vcoef = ncoef, vq = nq, vgz = ngz;
+        const bool inbox = nbox;
+        V4 hu = vzero(), hr = vzero();
+        const bool more = z + 1 < zend;
+        if (more) {  // queue head (plane z+R+1) and the next plane's operands
+            const long long ph = zoff + (long long)(R + 1) * L.plane + offl;
+            hu = ldg_v4(uc + ph, true);
+            if (SQ) hr = ldg_v4(den + ph, true);
+            fetch(z + 1);
+        }
+        const long long pz = zoff + off;
+        zoff += L.plane;
+
+        // z axis: queues (first-derivative sums start at their k = 1 term)
+        const V4 u0 = qu[slot(0)];
+        V4 sdz = vs0(u0), fuz, frz;
+#pragma unroll
+        for (int k = 1; k <= R; k++) {
+            const V4 a = qu[slot(k)], b = qu[slot(-k)];
+            sdz = vs(k, vadd(a, b), sdz);
+            if (VD) {
+                fuz = vw(k == 1, k, vsub(a, b), fuz);
+                if (SQ) {
+                    const V4 pa = lds_v4(sq + slot(k) * kThreads);
+                    const V4 pb = lds_v4(sq + slot(-k) * kThreads);
+                    frz = vw(k == 1, k, vsub(pa, pb), frz);
+                }
+            }
+        }
+        V4 rho0 = vzero();
+        if (SQ) rho0 = lds_v4(sq + slot(0) * kThreads);
+
+        const bool ok = mbar_wait(&bars[stage], parity);
+        if (!ok) s_abort = 1;
+        if (ok) {
+            const float* tu = tiles + stage * VT::STRIDE + (warp + R) * TW + 4 * lane;
+            const float* tr = tiles + (kStages + stage) * VT::STRIDE + (warp + R) * TW + 4 * lane;
+            // x axis: rows x +- k of the tile, this thread's 4 columns
+            V4 sdx = vs0(u0), fux, frx;
+#pragma unroll
+            for (int k = 1; k <= R; k++) {
+                const V4 a = lds_v4(tu + k * TW + HY);
+                const V4 b = lds_v4(tu - k * TW + HY);
+                sdx = vs(k, vadd(a, b), sdx);
+                if (VD) {
+                    fux = vw(k == 1, k, vsub(a, b), fux);
+                    const V4 ra = lds_v4(tr + k * TW + HY);
+                    const V4 rb = lds_v4(tr - k * TW + HY);
+                    frx = vw(k == 1, k, vsub(ra, rb), frx);
+                }
+            }
+            // y axis on pairs: the window's pairs starting at even offsets
+            // are the loaded 64-bit halves; odd offsets are repacked once
+            V4 sdy, fuy, fry;
+            {
+                P2 ev[2 * NC], od[2 * NC - 1];
+                YWindow<NC>::load(tu, ev, od);
+                P2 s[2], g[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    s[h] = mul2(w2[0], h ? u0.hi : u0.lo);
+#pragma unroll
+                    for (int k = 1; k <= R; k++) {
+                        const P2 a = YWindow<NC>::at(ev, od, HY + 2 * h + k);
+                        const P2 b = YWindow<NC>::at(ev, od, HY + 2 * h - k);
+                        s[h] = fma2(w2[k], add2(a, b), s[h]);
+                        if (VD)
+                            g[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), g[h]);
+                    }
+                }
+                sdy = {s[0], s[1]};
+                fuy = {g[0], g[1]};
+                if (VD) {
+                    YWindow<NC>::load(tr, ev, od);
+                    if (GZ) rho0 = {ev[HY / 2], ev[HY / 2 + 1]};
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+#pragma unroll
+                        for (int k = 1; k <= R; k++) {
+                            const P2 a = YWindow<NC>::at(ev, od, HY + 2 * h + k);
+                            const P2 b = YWindow<NC>::at(ev, od, HY + 2 * h - k);
+                            g[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), g[h]);
+                        }
+                    }
+                    fry = {g[0], g[1]};
+                }
+            }
+            // combine (reference order y, x, z) and update, on pairs
+            V4 lap = vmul({PW.ih2[2]}, sdy);
+            lap = vfma({PW.ih2[1]}, sdx, lap);
+            lap = vfma({PW.ih2[0]}, sdz, lap);
+            if (VD) {
+                const V4 my = {mul2(fuy.lo, fry.lo), mul2(fuy.hi, fry.hi)};
+                V4 cross = vmul({PW.s1[2]}, my);
+                cross = vfma({PW.s1[1]}, {mul2(fux.lo, frx.lo), mul2(fux.hi, frx.hi)}, cross);
+                if (GZ)
+                    cross = {fma2(fuz.lo, vgz.lo, cross.lo), fma2(fuz.hi, vgz.hi, cross.hi)};
+                else
+                    cross = vfma({PW.s1[0]}, {mul2(fuz.lo, frz.lo), mul2(fuz.hi, frz.hi)}, cross);
+                const float4 rr = to_f4(rho0);
+                const V4 inv = from_f4(make_float4(rcp_approx(rr.x), rcp_approx(rr.y),
+                                                   rcp_approx(rr.z), rcp_approx(rr.w)));
+                // lap -= cross / rho
+                lap = {fma2(sub2({0ull}, cross.lo), inv.lo, lap.lo),
+                       fma2(sub2({0ull}, cross.hi), inv.hi, lap.hi)};
+            }
+            // a = 2 u - (1 - q) u_prev;  b = a / (1 + q);  u_next = b + C lap
+            const P2 one{PW.one};
+            V4 a = {fma2(sub2(vq.lo, one), vprev.lo, add2(u0.lo, u0.lo)),
+                    fma2(sub2(vq.hi, one), vprev.hi, add2(u0.hi, u0.hi))};
+            if (!inbox) {
+                const float4 qq = to_f4(vq);
+                const V4 rq = from_f4(make_float4(
+                    rcp_approx(1.f + qq.x), rcp_approx(1.f + qq.y),
+                    rcp_approx(1.f + qq.z), rcp_approx(1.f + qq.w)));
+                a = {mul2(a.lo, rq.lo), mul2(a.hi, rq.hi)};
+            }
+            const V4 out = {fma2(lap.lo, vcoef.lo, a.lo), fma2(lap.hi, vcoef.hi, a.hi)};
+            if (full) {
+                *reinterpret_cast<ulonglong2*>(un + pz) = make_ulonglong2(out.lo.v, out.hi.v);
+            } else if (any) {
+                const float4 o = to_f4(out);
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    if (y0 + v < ylim) un[pz + v] = comp(o, v);
+            }
+        }
+        __syncthreads();  // the stage is free again; abort is uniform here
+        if (s_abort) {
+            aborted_at = it;
+            return false;
+        }
+        if (threadIdx.x == 0 && z + kStages < zend) {
+            issue(z + kStages, stage);
+            issued++;
+        }
+        // plane z - R leaves the queues; plane z + R + 1 takes its slot
+        if (more) {
+            qu[slot(-R)] = hu;
+            if (SQ) sts_v4(sq + slot(-R) * kThreads, hr);
+        }
+        return true;
+    };
+
+    for (int m = 0; zbeg + QN * m < zend; m++) {
+#pragma unroll
+        for (int J = 0; J < QN; J++) {
+            const int z = zbeg + QN * m + J;
+            if (z >= zend || !plane_step(z, J, m)) break;
+        }
+        if (aborted_at >= 0) break;
+    }
+    if (aborted_at >= 0 && threadIdx.x == 0) {
+        atomicExch(err, SIMWAVE_E_TIMEOUT);
+        for (int p = aborted_at; p < issued; p++)
+            mbar_wait(&bars[p % kStages], (unsigned)((p / kStages) & 1));
+    }
+}
+
 // ---- host side ---------------------------------------------------------------
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -824,13 +1259,57 @@ void launch_vec(float* un, const float* uc, const float* up, const float* coefC,
         L, W, (int)cur_slot, chunk, zb, ctx.err);
 }
 
+template <int R, bool VD, int MINB, bool GZ>
+void launch_vecp(float* un, const float* uc, const float* up, const float* coefC,
+                 const float* den, const float* coefQ, const Layout& L, const Weights<float>& W,
+                 const TiledContext& ctx, cudaStream_t st) {
+    auto kernel = stencil3d_vec4p<R, VD, MINB, GZ>;
+    static bool configured[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t smem = vec_smem_bytes<R, VD, VD && !GZ>();
+    if (!configured[dev & 63]) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured[dev & 63] = true;
+    }
+    const int ty = (int)((L.ny - 2 * R + 127) / 128);
+    const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
+    const int nzi = (int)(L.nz - 2 * R);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
+    const int zsplit = (nzi + chunk - 1) / chunk;
+    const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
+    ZeroBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
+               ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
+    dim3 grid(ty, tx, zsplit);
+    kernel<<<grid, kThreads, smem, st>>>(
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_u_vec),
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_vec), un, uc, up, coefC, den, coefQ,
+        ctx.coefGz, L, W, pair_weights(W), (int)cur_slot, chunk, zb, ctx.err);
+}
+
+// The packed kernel with the density z term from ctx.coefGz where the run
+// formed it, else from the shared-memory queue.
+template <int R, bool VD, int MINB>
+void launch_vecp_any(float* un, const float* uc, const float* up, const float* coefC,
+                     const float* den, const float* coefQ, const Layout& L,
+                     const Weights<float>& W, const TiledContext& ctx, cudaStream_t st) {
+    if (VD && ctx.coefGz)
+        launch_vecp<R, VD, MINB, VD>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+    else
+        launch_vecp<R, VD, MINB, false>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+}
+
 template <int R, bool VD>
 void launch_vec_policy(int policy, float* un, const float* uc, const float* up,
                        const float* coefC, const float* den, const float* coefQ,
                        const Layout& L, const Weights<float>& W, const TiledContext& ctx,
                        cudaStream_t st) {
+    // AUTO: the packed kernel, except constant density at order 2 where the
+    // plain float4 kernel measured faster (0.224 vs 0.265 ms, 408^3 grid)
     if (policy == SIMWAVE_POLICY_AUTO)
-        policy = (VD && R >= 3) ? SIMWAVE_POLICY_VEC_SMEMQ : SIMWAVE_POLICY_VEC_2CTA_ROT;
+        policy = (!VD && R == 1) ? SIMWAVE_POLICY_VEC_2CTA : SIMWAVE_POLICY_VEC_PACKED;
     switch (policy) {
         case SIMWAVE_POLICY_VEC_2CTA:
             return launch_vec<R, VD, 2, false, false>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
@@ -840,11 +1319,27 @@ void launch_vec_policy(int policy, float* un, const float* uc, const float* up,
             return launch_vec<R, VD, 2, VD, true>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
         case SIMWAVE_POLICY_VEC_2CTA_ROT:
             return launch_vec<R, VD, 2, false, true>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+        case SIMWAVE_POLICY_VEC_PACKED:
+            return launch_vecp_any<R, VD, 2>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
+        case SIMWAVE_POLICY_VEC_PACKED_1CTA:
+            return launch_vecp_any<R, VD, 1>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
         default:  // SIMWAVE_POLICY_VEC_1CTA_ROT
             return launch_vec<R, VD, 1, false, true>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
     }
 }
 }  // namespace
+
+void form_density_z(const float* den, float* gz, const Layout& L, const Weights<float>& W,
+                    cudaStream_t st) {
+    form_density_z<<<device_info().sms * 8, 256, 0, st>>>(den, gz, L, W);
+}
+
+bool wants_density_z(const Layout& L, bool vd) {
+    const int p = kernel_policy();
+    return vd && L.dim == 3 && L.r <= 4 &&
+           (p == SIMWAVE_POLICY_AUTO || p == SIMWAVE_POLICY_VEC_PACKED ||
+            p == SIMWAVE_POLICY_VEC_PACKED_1CTA);
+}
 
 void form_coefficients(const float* vel, const float* damp, float* C, float* Q,
                        long long n, float dt, cudaStream_t st) {

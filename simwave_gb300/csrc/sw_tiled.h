@@ -21,6 +21,7 @@ struct TiledContext {
     int* err = nullptr;
     const float* coefC = nullptr;  // per-point coefficients (same layout as u)
     const float* coefQ = nullptr;
+    const float* coefGz = nullptr; // density z term (variable density), or null
     void* scratch = nullptr;       // the run's coefficient/zero-box scratch
 };
 
@@ -50,6 +51,12 @@ bool tiled2d_supported(const Layout& L);
 void tiled2d_launch(const Layout& L, bool vd, float* un, const float* uc, const float* up,
                     const float* C, const float* Q, const float* den,
                     const Weights<float>& W, const int* zero_box, cudaStream_t st);
+
+// gz = s1_z * sum_k c1_k (rho(z+k) - rho(z-k)) at interior points (3D).
+void form_density_z(const float* den, float* gz, const Layout& L, const Weights<float>& W,
+                    cudaStream_t st);
+// Whether the selected 3D kernel reads gz (then the run forms it).
+bool wants_density_z(const Layout& L, bool vd);
 
 int kernel_policy();
 void set_kernel_policy(int policy);

@@ -161,7 +161,8 @@ def test_repeated_calls_are_deterministic():
 
 
 POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3,
-            "vec_smemq": 4, "vec_2cta_rot": 5, "vec_1cta_rot": 6}
+            "vec_smemq": 4, "vec_2cta_rot": 5, "vec_1cta_rot": 6, "vec_packed": 7,
+            "vec_packed_1cta": 8}
 
 
 @pytest.mark.parametrize("policy", list(POLICIES))
