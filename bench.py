@@ -274,7 +274,10 @@ def served_leg(nreq=40):
         lat.append(done - a)
     seq = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
            "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
-           "shots_per_s": round(len(reqs) / (done - arrivals[0]), 2)}
+           "shots_per_s": round(len(reqs) / (done - arrivals[0]), 2),
+           "service_s_by_kind": {k: round(sum(sv for r, sv in zip(reqs, service)
+                                              if r.kind == k), 3)
+                                 for k in sorted({r.kind for r in reqs})}}
     # served: continuous batching
     torch.cuda.synchronize()
     server = ShotServer(epoch_steps=64)
@@ -479,15 +482,22 @@ def cpu_sample(steps, threads=None, n=384):
 
 # ---------------------------------------------------------------------------
 
-def dist_setup(n_gpus):
+def dist_setup(n_gpus, backend=None):
+    """Rank, world size and local rank from the launcher's environment; one
+    process per GPU (NCCL), or gloo where no GPU is visible. Ranks are
+    independent replicas: the only collectives are the timing barrier and
+    the max over ranks."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -502,9 +512,16 @@ def max_over_ranks(value, world):
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_rate(units_per_rank, world, ms_per_step):
+    """Whole-job rate (units / s, in 1e9) of `world` replicas that each
+    process `units_per_rank` per step, timed by the slowest rank."""
+    return units_per_rank * world / (ms_per_step / 1e3) / 1e9
 
 
 def run_reference_arm(args):
@@ -617,7 +634,7 @@ def main():
     clock_info = clocks.stop()
     total_ms = max_over_ranks(float(np.sum(ms)), world)
     ms_per_step = total_ms / args.steps
-    value = updates * world / (ms_per_step / 1e3) / 1e9
+    value = aggregate_rate(updates, world, ms_per_step)
 
     # stencil kernel time: events around each stencil launch, same stream
     dp.reset()

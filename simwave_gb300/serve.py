@@ -8,16 +8,19 @@ host when the shot completes.
 * 2D float32 shots join a running ``BatchEngine``: every epoch advances all
   admitted 2D shots by ``epoch_steps`` time steps in one graph-captured
   sequence, and newly admitted shots join at the next epoch.
-* Other shots (3D, or float64) run through the device entry on a
-  low-priority stream, shortest first (interior updates), at most
-  ``inflight`` queued at a time; each one fills the GPU on its own, so running
-  them side by side would only delay all of them. The 2D epochs run on a
-  high-priority stream and overlap them at block granularity.
+* Other shots (3D, or float64) run through the device entry on their own
+  stream, shortest first (interior updates), at most ``inflight`` queued at a
+  time, and only while no 2D shot is in the batch: each such shot fills the
+  GPU on its own, and its long-running blocks would hold every SM between the
+  batch's short launches (stream priority only orders blocks not yet
+  placed), delaying every 2D step; the batch, whose shots are the shorter
+  jobs, goes first.
 
 Latency of a request = completion time - arrival time (queueing, upload,
 compute and shot-record download included).
 """
 import collections
+import concurrent.futures
 import time
 
 import numpy as np
@@ -50,6 +53,7 @@ class Request:
         self.arrival = arrival
         self.tag = tag
         self.admitted = None
+        self.started = None  # launch time of a stream-run shot
         self.completed = None
         self.problem = None
         self.shot_record = None
@@ -58,6 +62,9 @@ class Request:
         v = kwargs["velocity_model"]
         self.batchable = v.ndim == 2 and v.dtype == np.float32
         self.updates = int(np.prod(v.shape)) * int(kwargs["end_timestep"])
+        self.kind = "{}d".format(v.ndim)
+        self._staged = None  # future of (DeviceProblem, upload event)
+        self._uploaded = None  # event the device copies complete at
 
     @property
     def latency(self):
@@ -81,8 +88,13 @@ class ShotServer:
         lo, hi = torch.cuda.Stream.priority_range()
         self.epoch_stream = torch.cuda.Stream(self.device, priority=hi)
         self.shot_stream = torch.cuda.Stream(self.device, priority=lo)
+        # uploads of stream-run shots happen on a worker thread and stream
+        # so the serving loop keeps stepping the batch meanwhile
+        self.stage_stream = torch.cuda.Stream(self.device)
+        self._stager = concurrent.futures.ThreadPoolExecutor(max_workers=1)
         self.inflight = max(int(inflight), 1)
         self.pending = collections.deque()
+        self.staging = []    # admitted requests whose device copies are being made
         self.active2d = {}   # shot id -> request
         self.ready = []      # admitted stream-run shots not yet launched
         self.active = []     # (request, event) of launched stream-run shots
@@ -107,26 +119,52 @@ class ShotServer:
                     break
             self.pending.popleft()
             req.admitted = time.perf_counter()
-            req.problem = DeviceProblem(req.kwargs, device=self.device)
             self.in_use += req.bytes
-            if req.batchable:
-                sid = self.engine.add(req.problem)
-                self.active2d[sid] = req
-            else:
-                self.ready.append(req)
+            req._staged = self._stager.submit(self._stage, req)
+            self.staging.append(req)
             admitted = True
-        # the uploads above were queued on the current stream
-        if admitted:
-            self.epoch_stream.wait_stream(torch.cuda.current_stream(self.device))
-            self.shot_stream.wait_stream(torch.cuda.current_stream(self.device))
+        self._collect()
         self._launch()
         return admitted
 
+    def _collect(self):
+        """Move requests whose device copies are ready into the batch or the
+        stream-run queue."""
+        still = []
+        for req in self.staging:
+            if not req._staged.done():
+                still.append(req)
+                continue
+            req.problem, uploaded = req._staged.result()
+            req._staged = None
+            if req.batchable:
+                self.epoch_stream.wait_event(uploaded)
+                sid = self.engine.add(req.problem)
+                self.active2d[sid] = req
+            else:
+                req._uploaded = uploaded
+                self.ready.append(req)
+        self.staging = still
+
+    def _stage(self, req):
+        """Worker thread: the request's device copies, on the staging
+        stream; returns the problem and the event its uploads complete at."""
+        with torch.cuda.device(self.device), torch.cuda.stream(self.stage_stream):
+            prob = DeviceProblem(req.kwargs, device=self.device)
+            ev = torch.cuda.Event()
+            ev.record(self.stage_stream)
+        return prob, ev
+
     def _launch(self):
-        """Queue the shortest admitted stream-run shots on the shot stream."""
-        while self.ready and len(self.active) < self.inflight:
+        """Queue the shortest admitted stream-run shots on the shot stream
+        (none while the 2D batch has shots or is about to get some)."""
+        busy2d = bool(self.active2d) or any(r.batchable for r in self.staging)
+        while self.ready and len(self.active) < self.inflight and not busy2d:
             req = min(self.ready, key=lambda r: r.updates)
             self.ready.remove(req)
+            self.shot_stream.wait_event(req._uploaded)
+            req._uploaded = None
+            req.started = time.perf_counter()
             req.problem.run(self.shot_stream)
             ev = torch.cuda.Event()
             ev.record(self.shot_stream)
@@ -193,7 +231,7 @@ class ShotServer:
                 self.engine.run(self.epoch_steps, stream=self.epoch_stream)
                 # bound the queue ahead of the host: wait for this epoch
                 self.epoch_stream.synchronize()
-            elif self.active:
+            elif self.active or self.staging:
                 time.sleep(0.0005)
             elif self.pending:
                 wait = self.pending[0].arrival - time.perf_counter()
@@ -203,14 +241,24 @@ class ShotServer:
         return requests
 
     def close(self):
+        self._stager.shutdown(wait=True)
         self.engine.close()
 
 
 def latency_summary(requests):
     lat = np.array([r.latency for r in requests], dtype=np.float64)
     span = max(r.completed for r in requests) - min(r.arrival for r in requests)
+    t0 = min(r.arrival for r in requests)
+    kinds = {}
+    for kind in sorted({r.kind for r in requests}):
+        sub = [r for r in requests if r.kind == kind]
+        kl = np.array([r.latency for r in sub])
+        kinds[kind] = {"shots": len(sub),
+                       "p50_ms": round(float(np.percentile(kl, 50)) * 1e3, 2),
+                       "max_ms": round(float(kl.max()) * 1e3, 2),
+                       "last_done_s": round(max(r.completed for r in sub) - t0, 3)}
     return {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
             "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
             "mean_ms": round(float(lat.mean()) * 1e3, 2),
             "shots_per_s": round(len(requests) / span, 2),
-            "shots": len(requests)}
+            "shots": len(requests), "by_kind": kinds}
