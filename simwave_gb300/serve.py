@@ -75,7 +75,7 @@ class ShotServer:
     """Serve requests with continuous batching on one GPU."""
 
     def __init__(self, hbm_budget=None, epoch_steps=64, inflight=2, device="cuda",
-                 tile_rows=None):
+                 tile_rows=None, reserve_bytes=0, stage_workers=2):
         self.device = torch.device(device)
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
@@ -91,7 +91,13 @@ class ShotServer:
         # uploads of stream-run shots happen on a worker thread and stream
         # so the serving loop keeps stepping the batch meanwhile
         self.stage_stream = torch.cuda.Stream(self.device)
-        self._stager = concurrent.futures.ThreadPoolExecutor(max_workers=1)
+        self._stager = concurrent.futures.ThreadPoolExecutor(max_workers=max(stage_workers, 1))
+        if reserve_bytes:
+            # keep device memory in the caching allocator (whose free blocks
+            # belong to the stream they were allocated on) so that staging
+            # carves problems out of it instead of calling cudaMalloc
+            with torch.cuda.stream(self.stage_stream):
+                torch.empty(int(reserve_bytes), dtype=torch.uint8, device=self.device)
         self.inflight = max(int(inflight), 1)
         self.pending = collections.deque()
         self.staging = []    # admitted requests whose device copies are being made
@@ -103,6 +109,16 @@ class ShotServer:
     # -- admission ----------------------------------------------------------
     def submit(self, request):
         self.pending.append(request)
+
+    def prepare(self, requests):
+        """Make the device copies of known requests ahead of serving them
+        (their memory is counted at admission as usual); returns when done."""
+        for req in requests:
+            if req._staged is None and req.problem is None:
+                req._staged = self._stager.submit(self._stage, req)
+        for req in requests:
+            if req._staged is not None:
+                req._staged.result()
 
     def _admit(self, now):
         admitted = False
@@ -120,7 +136,8 @@ class ShotServer:
             self.pending.popleft()
             req.admitted = time.perf_counter()
             self.in_use += req.bytes
-            req._staged = self._stager.submit(self._stage, req)
+            if req._staged is None:
+                req._staged = self._stager.submit(self._stage, req)
             self.staging.append(req)
             admitted = True
         self._collect()

@@ -84,6 +84,7 @@ def test_stream_shots_run_shortest_first():
                             seed=70 + i, nrec=3)
         reqs.append(Request(kw, 0.0, tag=i))
     server = ShotServer(inflight=1)
+    server.prepare(reqs)  # all staged: the order is the server's choice alone
     server.serve(reqs, timeout=300)
     server.close()
     order = [r.tag for r in sorted(reqs, key=lambda r: r.completed)]
