@@ -23,6 +23,15 @@ Gpts/s, whole job over all ranks.
   cpu_baseline the CPU checker (C restatement, OpenMP, all host cores) on a
               bounded sample of the same workload (fewer time steps)
 
+Extra legs in the same line (rank 0): `batched` (96 2D shots advanced
+together vs back-to-back plain device calls), `served` (a Poisson stream of
+mixed 2D/3D requests through the continuous-batching server vs the same
+requests through the drop-in one after another: p50/p99, shots/s) and
+`gradient` (misfit and velocity gradient of 16 2D shots with checkpointed
+recomputation, plus a finite-difference check); `--no-batched`,
+`--no-served`, `--no-gradient` skip them, `--served` / `--gradient` run one
+alone.
+
 `--impl reference` times the reference's CPU algorithm (the C restatement)
 on the host cores instead and prints the same metric.
 Multi-GPU (torchrun): independent replicas, one shot per rank, no collective
@@ -340,7 +349,7 @@ def config5_arguments(vel, dt=None, nshots=16, damping_points=50):
     return out, float(tm.dt)
 
 
-def gradient_leg(nshots=16, steps=1, interval=None):
+def gradient_leg(nshots=16, steps=1, interval=None, workers=4):
     """The inversion workload: L2 misfit and its velocity gradient over the
     shots at the smoothed model, observed data from the true model. Reports
     shots/s, the point updates of the forward, recomputation and adjoint
@@ -367,7 +376,7 @@ def gradient_leg(nshots=16, steps=1, interval=None):
     times = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        loss, grad = misfit_gradient(v0, problems, observed, K)
+        loss, grad = misfit_gradient(v0, problems, observed, K, workers=workers)
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
     best = min(times)
@@ -392,6 +401,7 @@ def gradient_leg(nshots=16, steps=1, interval=None):
                         "so 8, 8 Hz Ricker, 1701 receivers, tf 3.0 s, T %d, "
                         "checkpoint interval %d" % (nshots, T, K),
             "grid": list(problems[0].shape), "timesteps": T, "interval": K,
+            "workers": workers,
             "seconds": round(best, 4), "shots_per_s": round(nshots / best, 3),
             "gpts_per_s_3pass": round(3.0 * nshots * interior * T / best / 1e9, 2),
             "misfit": loss, "fd_directional": fd, "adjoint_directional": ad,
@@ -579,6 +589,10 @@ def main():
                     help="run only the served (continuous batching) leg")
     ap.add_argument("--gradient", action="store_true",
                     help="run only the inversion (velocity gradient) leg")
+    ap.add_argument("--no-served", action="store_true",
+                    help="skip the served leg of the default line")
+    ap.add_argument("--no-gradient", action="store_true",
+                    help="skip the inversion leg of the default line")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -687,9 +701,20 @@ def main():
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": round(e2e_total / len(e2e_ms), 3)}
 
-    batched = None
-    if not args.no_batched:
-        batched = batched_leg()
+    def leg(fn, **kw):
+        """An extra leg's JSON; its failure is reported, not fatal to the line."""
+        try:
+            return fn(**kw)
+        except Exception as exc:  # noqa: BLE001 - reported in the JSON line
+            return {"error": "%s: %s" % (type(exc).__name__, exc)}
+
+    batched = served = gradient = None
+    if rank == 0 and not args.no_batched:
+        batched = leg(batched_leg)
+    if rank == 0 and not args.no_served:
+        served = leg(served_leg)
+    if rank == 0 and not args.no_gradient:
+        gradient = leg(gradient_leg, steps=1)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -724,6 +749,8 @@ def main():
             "clocks": clock_info,
             "cpu_baseline": cpu,
             "batched": batched,
+            "served": served,
+            "gradient": gradient,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

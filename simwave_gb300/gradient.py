@@ -83,20 +83,52 @@ def shot_record(velocity, problem, interval=None):
     return _ShotRecord.apply(velocity, problem, int(interval or default_interval(steps)))
 
 
-def misfit_gradient(velocity, problems, observed, interval=None):
+def misfit_gradient(velocity, problems, observed, interval=None, workers=4):
     """L2 misfit over shots and its velocity gradient.
 
     ``velocity``: the extended grid (float32 tensor on the device);
     ``problems``: one ``DeviceProblem`` per shot on that grid; ``observed``:
     one shot record per shot (tensor or array, same shape as the record).
-    Returns ``(misfit, gradient)`` with the gradient on the extended grid.
+    Shots are independent: up to ``workers`` of them run at once, each from
+    its own host thread on its own CUDA stream (a shot's launches are short,
+    so one host thread alone leaves the GPU idle between them). Returns
+    ``(misfit, gradient)`` with the gradient on the extended grid.
     """
-    v = velocity.detach().clone().requires_grad_(True)
+    import concurrent.futures
+    v0 = velocity.detach()
+    device = v0.device
+    main = torch.cuda.current_stream(device)
+
+    def one(args):
+        prob, obs, stream = args
+        stream.wait_stream(main)
+        with torch.cuda.device(device), torch.cuda.stream(stream):
+            v = v0.clone().requires_grad_(True)
+            obs = torch.as_tensor(obs, dtype=torch.float32, device=device)
+            rec = shot_record(v, prob, interval)
+            loss = 0.5 * torch.sum((rec - obs) ** 2)
+            (g,) = torch.autograd.grad(loss, v)
+            done = torch.cuda.Event()
+            done.record(stream)
+        return float(loss.detach()), g, done
+
+    n = max(1, min(int(workers), len(problems)))
+    streams = [torch.cuda.Stream(device) for _ in range(n)]
+    jobs = [(p, o, streams[i % n]) for i, (p, o) in enumerate(zip(problems, observed))]
+    if n == 1:
+        results = [one(j) for j in jobs]
+    else:
+        with concurrent.futures.ThreadPoolExecutor(max_workers=n) as pool:
+            # shot i goes to stream i mod n; each worker thread takes whole
+            # shots, so two shots never share a stream at the same time
+            by_stream = [[j for j in jobs if j[2] is s] for s in streams]
+            futs = [pool.submit(lambda js: [one(j) for j in js], js) for js in by_stream]
+            results = [r for f in futs for r in f.result()]
     total = 0.0
-    for prob, obs in zip(problems, observed):
-        obs = torch.as_tensor(obs, dtype=torch.float32, device=v.device)
-        rec = shot_record(v, prob, interval)
-        loss = 0.5 * torch.sum((rec - obs) ** 2)
-        loss.backward()
-        total += float(loss.detach())
-    return total, v.grad
+    grad = torch.zeros_like(v0)
+    for loss, g, done in results:
+        main.wait_event(done)
+        g.record_stream(main)  # made on a worker stream, read on this one
+        grad += g
+        total += loss
+    return total, grad
