@@ -301,6 +301,97 @@ def served_leg(nreq=40):
             "speedup_shots_per_s": round(served["shots_per_s"] / seq["shots_per_s"], 2)}
 
 
+def config1_arguments():
+    """The reference README's 2D case: 512^2 model (1500 m/s above row 100,
+    2000 below) interpolated onto the 513^2 grid of a 5120 m box at 10 m,
+    order 4, no damping layer, boundaries (null_neumann, null_dirichlet,
+    none, null_dirichlet), tf 1.0 s (T 328), 10 Hz Ricker at (2560, 2560)
+    with window radius 1, 512 receivers at z = 2560 m, x = 0..5110 m."""
+    import simwave_gb300 as sw
+    vel = np.full((512, 512), 2000.0, dtype=np.float32)
+    vel[:100] = 1500.0
+    sm = sw.SpaceModel((0.0, 5120.0, 0.0, 5120.0), (10.0, 10.0), vel, space_order=4,
+                       dtype=np.float32)
+    sm.config_boundary(damping_length=0.0, boundary_condition=(
+        "null_neumann", "null_dirichlet", "none", "null_dirichlet"))
+    tm = sw.TimeModel(space_model=sm, tf=1.0, saving_stride=0)
+    src = sw.Source(sm, coordinates=[(2560.0, 2560.0)], window_radius=1)
+    rec = sw.Receiver(sm, coordinates=[(2560.0, x) for x in range(0, 5112, 10)],
+                      window_radius=1)
+    return sw.Solver(sm, tm, src, rec, sw.RickerWavelet(10.0, tm)).forward_arguments()
+
+
+def config1_leg(reps=20):
+    """Config 1 (L2- and launch-bound): Gpts/s of plain device calls, of the
+    same shot through the graph-captured batch engine, of the drop-in with
+    host buffers, and of the CPU checker on the full run (with the relative
+    L2 difference of the shot record against it)."""
+    import contextlib
+    import io
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU baseline and checker of this leg
+    from simwave_gb300.backend.middleware import Middleware
+    from simwave_gb300.batch import BatchEngine
+    from simwave_gb300.device import DeviceProblem
+    kw = config1_arguments()
+    pts, updates = interior_updates(kw)
+    dp = DeviceProblem(kw)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            dp.reset()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    plain_ms = timed(lambda: dp.run())
+    eng = BatchEngine()
+
+    def batched():
+        sid = eng.add(dp)
+        eng.run(dp.timesteps)
+        eng.release(sid)
+    batch_ms = timed(batched)
+    eng.close()
+    dp.reset()
+    dp.run()
+    dp.status()
+    gpu_rec = dp.shot_record_numpy()
+    mw = Middleware()
+    e2e = []
+    for i in range(reps // 4 + 1):
+        k = dict(kw, u_full=np.zeros_like(kw["u_full"]), shot_record=np.zeros_like(kw["shot_record"]))
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(io.StringIO()):
+            mw.exec("forward", **k)
+        if i:
+            e2e.append(1e3 * (time.perf_counter() - t0))
+    k = dict(kw, u_full=np.zeros_like(kw["u_full"]), shot_record=np.zeros_like(kw["shot_record"]))
+    t0 = time.perf_counter()
+    _, cpu_rec, _ = oracle.forward("port", **k)
+    cpu_s = time.perf_counter() - t0
+    rel = float(np.linalg.norm(gpu_rec - cpu_rec) / np.linalg.norm(cpu_rec))
+    gp = lambda ms: round(updates / (ms / 1e3) / 1e9, 2)  # noqa: E731
+    return {"workload": "2D CD so4 513^2 (517^2 extended), T %d, 512 receivers"
+                        % kw["end_timestep"],
+            "updates": updates, "plain_ms": round(plain_ms, 3), "plain_gpts": gp(plain_ms),
+            "graph_ms": round(batch_ms, 3), "graph_gpts": gp(batch_ms),
+            "e2e_ms": round(float(np.median(e2e)), 3), "e2e_gpts": gp(float(np.median(e2e))),
+            "cpu_port_s": round(cpu_s, 3), "cpu_port_gpts": round(updates / cpu_s / 1e9, 3),
+            "cpu_threads": os.cpu_count(),
+            "shot_record_rel_l2_vs_cpu": rel,
+            "hbm_note": "16 B/update algorithmic; the 5 MB state stays in L2"}
+
+
 def config5_models(seed=5):
     """The inversion workload's models on a (351, 1701) grid of 10 m (nz = 351,
     nx = 1701): 12 layers from 1500 to 5500 m/s cut by two dipping faults
@@ -708,7 +799,9 @@ def main():
         except Exception as exc:  # noqa: BLE001 - reported in the JSON line
             return {"error": "%s: %s" % (type(exc).__name__, exc)}
 
-    batched = served = gradient = None
+    batched = served = gradient = plain2d = None
+    if rank == 0:
+        plain2d = leg(config1_leg)
     if rank == 0 and not args.no_batched:
         batched = leg(batched_leg)
     if rank == 0 and not args.no_served:
@@ -748,6 +841,7 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clock_info,
             "cpu_baseline": cpu,
+            "plain_2d": plain2d,
             "batched": batched,
             "served": served,
             "gradient": gradient,

@@ -227,6 +227,11 @@ typedef struct simwave_problem {
 
 #define SIMWAVE_FLAG_GENERIC_KERNEL 4u  /* force the one-thread-per-point
                                            stencil (testing and comparison) */
+#define SIMWAVE_FLAG_STEP_LAUNCHES 8u   /* 2D float32: launch each step's
+                                           kernels separately even where the
+                                           whole run would go in one persistent
+                                           launch (grids up to 1.5 M interior
+                                           points) -- testing and timing */
 
 /* Preferred layout of the fastest axis for a grid of `fastest_extent`
  * points at `space_order` and `precision` bytes: writes the row pitch and
@@ -341,7 +346,8 @@ typedef struct simwave_stats {
     size_t stencil_launches;  /* stencil kernel launches */
     size_t kernel_launches;   /* all kernel launches of this library */
     size_t h2d_bytes, d2h_bytes;
-    int stencil_variant;      /* 0 generic, 1 tiled */
+    int stencil_variant;      /* 0 generic, 1 tiled, 2 tiled 2D, all steps
+                                 in one persistent launch */
 } simwave_stats;
 
 /* No reference counterpart (the reference returns only its wall time). */

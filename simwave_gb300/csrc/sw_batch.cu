@@ -771,7 +771,266 @@ static int guarded(F&& f) {
     }
 }
 
+// ---- persistent 2D forward: every step of one shot in one launch ----------
+//
+// Small 2D grids are bound by the start-up and drain of the six short
+// kernels of each step, not by their work (a 513^2 order-4 shot spends
+// about 20 us per step either way, with or without graph launches). One
+// cooperative launch runs all steps instead: per step, the tiles of the
+// stencil and the receiver gathers, then the sources, then the x and z
+// boundary phases, each phase separated by a grid barrier. The barrier
+// spins with a time limit: on expiry the block records SIMWAVE_E_TIMEOUT and
+// the kernel ends (blocks still inside a barrier time out the same way).
+
+struct Persist2D {
+    Layout L;
+    float* u;                 // slot 0
+    const int* slots;         // per step: next, cur, prev physical slots
+    int steps;
+    long long begin;
+    const float *C, *Q, *den;
+    const float *vel, *damp;  // source scaling, as the per-step path forms it
+    Weights<float> W;
+    ZeroBox2 zb;
+    Windows<float> src;
+    const float* wavelet;
+    size_t wavelet_count;
+    float dt;
+    Windows<float> rec;
+    float* receivers;
+    int bc[4];
+    int tiles_x, tiles_z, ntiles;
+    int fused;                // sources and edges by the owning tile (see below)
+    unsigned* bar;            // [0] arrivals, [1] generation (zeroed before launch)
+    int* err;
+};
+
+// Owner-computes part of a step for tile (tz, tx), after its stencil: the
+// source points in the tile (points of the halo belong to the nearest edge
+// tile), then the x edges of its rows if it is an x-edge tile, then the z
+// edges of its columns if it is a z-edge tile. Exact when the first and last
+// tiles hold at least r + 1 rows and columns: every boundary operation then
+// reads and writes points of one tile only, in the reference's order.
+__device__ void tile_sources_edges(const Persist2D& P, float* un, long long n, int tz, int tx) {
+    const Layout& L = P.L;
+    const int r = L.r;
+    const int nz = (int)L.nz, nx = (int)L.nx;
+    const int z_lo = tz == 0 ? 0 : r + 16 * tz;
+    const int z_hi = tz == P.tiles_z - 1 ? nz : r + 16 * (tz + 1);
+    const int x_lo = tx == 0 ? 0 : r + 128 * tx;
+    const int x_hi = tx == P.tiles_x - 1 ? nx : r + 128 * (tx + 1);
+    const float dt2 = P.dt * P.dt;
+    for (size_t s = 0; s < P.src.count; s++) {
+        const float w = wavelet_at(P.wavelet, P.wavelet_count, (size_t)n, P.src.count, s);
+        if (w == 0.f) continue;
+        const size_t* b = P.src.interval + s * 4;
+        if ((int)b[1] < z_lo || (int)b[0] >= z_hi || (int)b[3] < x_lo || (int)b[2] >= x_hi)
+            continue;
+        const float* v = P.src.values + P.src.offsets[s];
+        const long long total = window_size<2>(b);
+        for (long long t = threadIdx.x; t < total; t += blockDim.x) {
+            long long iz, ix, iy;
+            window_point<2>(b, t, iz, ix, iy);
+            const int z = (int)(b[0] + iz), x = (int)(b[2] + ix);
+            if (z < z_lo || z >= z_hi || x < x_lo || x >= x_hi) continue;
+            const float kws = window_weight<float, 2>(b, v, iz, ix, iy);
+            const long long p = L.at2(z, x);
+            const float vv = P.vel[p] * P.vel[p];
+            const float d = 1.f + P.damp[p] * P.dt * vv * 0.5f;
+            atomicAdd(un + p, dt2 * vv * kws * w / d);
+        }
+    }
+    __syncthreads();
+    // x edges (rows of this tile), then z edges (columns of this tile)
+    const int bx0 = P.bc[2], bx1 = P.bc[3], bz0 = P.bc[0], bz1 = P.bc[1];
+    if ((bx0 && tx == 0) || (bx1 && tx == P.tiles_x - 1)) {
+        const int r0 = max(z_lo, r), r1 = min(z_hi, nz - r);
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            if (tx == 0) apply_edge(un, L.at2(i, r), 1, r, bx0, -1);
+            if (tx == P.tiles_x - 1) apply_edge(un, L.at2(i, nx - r - 1), 1, r, bx1, +1);
+        }
+    }
+    __syncthreads();
+    if ((bz0 && tz == 0) || (bz1 && tz == P.tiles_z - 1)) {
+        const int c0 = max(x_lo, r), c1 = min(x_hi, nx - r);
+        for (int j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+            if (tz == 0) apply_edge(un, L.at2(r, j), L.pitch, r, bz0, -1);
+            if (tz == P.tiles_z - 1) apply_edge(un, L.at2(nz - r - 1, j), L.pitch, r, bz1, +1);
+        }
+    }
+    __syncthreads();
+}
+
+constexpr long long kBarrierCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+// Grid-wide barrier of the cooperative launch; false when the wait expired
+// (then the error word is set). Every block calls it the same number of
+// times; the generation is read before arriving so a flip is never missed.
+__device__ bool grid_barrier(unsigned* bar, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g) {
+                if (clock64() - t0 > kBarrierCycles || *(volatile int*)err) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (!ok) atomicCAS(err, 0, SIMWAVE_E_TIMEOUT);
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int R, bool VD, int TZ>
+__global__ void __launch_bounds__(kThreads)
+stencil2d_persistent(const Persist2D P) {
+    const Layout L = P.L;
+    float* tile = reinterpret_cast<float*>(sw_batch_smem);
+    const long long gthreads = (long long)gridDim.x * blockDim.x;
+    const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const float dt2 = P.dt * P.dt;
+    for (int i = 0; i < P.steps; i++) {
+        const long long n = P.begin + i;
+        float* un = P.u + (long long)P.slots[3 * i] * L.slot;
+        const float* uc = P.u + (long long)P.slots[3 * i + 1] * L.slot;
+        const float* up = P.u + (long long)P.slots[3 * i + 2] * L.slot;
+        // stencil tiles, then the receivers (they read u_cur only)
+        for (int t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
+            stencil2d_tile<R, VD, TZ>(tile, L, un, uc, up, P.C, P.Q, P.den, P.W, P.zb.b,
+                                      t / P.tiles_x, t % P.tiles_x);
+            __syncthreads();  // the tile buffer is restaged next
+            if (P.fused) tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x);
+        }
+        if (P.rec.count) {
+            float* row = P.receivers + (n - 1) * (long long)P.rec.count;
+            for (long long w = gtid >> 5; w < (long long)P.rec.count; w += gthreads >> 5) {
+                const float sum = gather_window<float, 2>(
+                    uc, L, P.rec.interval + w * 4, P.rec.values + P.rec.offsets[w], lane);
+                if (lane == 0) row[w] = sum;
+            }
+        }
+        if (!grid_barrier(P.bar, P.err)) return;
+        if (P.fused) continue;  // sources and edges were applied per tile
+        if (P.src.count) {
+            for (size_t sidx = blockIdx.x; sidx < P.src.count; sidx += gridDim.x) {
+                const float w = wavelet_at(P.wavelet, P.wavelet_count, (size_t)n, P.src.count,
+                                           sidx);
+                if (w != 0.f)
+                    inject_window<float, 2>(un, P.vel, P.damp, L,
+                                            P.src.interval + sidx * 4,
+                                            P.src.values + P.src.offsets[sidx], w, P.dt, dt2,
+                                            threadIdx.x, blockDim.x);
+            }
+            if (!grid_barrier(P.bar, P.err)) return;
+        }
+        // boundary phases in the reference's order: x edges, then z edges
+        for (int a = 1; a >= 0; a--) {
+            const int b0 = P.bc[2 * a], b1 = P.bc[2 * a + 1];
+            if (!b0 && !b1) continue;
+            const long long lines = boundary_lines(L, a);
+            for (long long t = gtid; t < lines; t += gthreads) boundary_line(un, L, a, b0, b1, t);
+            if (!grid_barrier(P.bar, P.err)) return;
+        }
+    }
+}
+
+template <int R, bool VD>
+static bool persistent_r(const Persist2D& P, cudaStream_t st) {
+    constexpr int TZ = 16;
+    constexpr int HX = (R + 3) & ~3;
+    const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
+    auto kernel = stencil2d_persistent<R, VD, TZ>;
+    static bool configured[64] = {};
+    int dev = 0;
+    SB_CUDA(cudaGetDevice(&dev));
+    if (!configured[dev & 63]) {
+        SB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     bytes));
+        configured[dev & 63] = true;
+    }
+    int coop = 0, sms = 0, per_sm = 0;
+    SB_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    SB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, bytes));
+    if (!coop || per_sm < 1) return false;
+    Persist2D A = P;
+    const int grid = std::max(1, std::min(P.ntiles, per_sm * sms));
+    void* args[] = {&A};
+    SB_CUDA(cudaMemsetAsync(P.bar, 0, 2 * sizeof(unsigned), st));
+    SB_CUDA(cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(kThreads), args,
+                                        (size_t)bytes, st));
+    return true;
+}
+
 }  // namespace batch
+
+bool persistent2d_launch(const Layout& L, bool vd, float* u, const int* slots, int steps,
+                         long long begin, const float* C, const float* Q, const float* den,
+                         const float* vel, const float* damp,
+                         const Weights<float>& W, const int* zero_box,
+                         const Windows<float>& src, const float* wavelet,
+                         size_t wavelet_count, float dt, const Windows<float>& rec,
+                         float* receivers, const int* bc, unsigned* bar, int* err,
+                         cudaStream_t st) {
+    if (!tiled2d_supported(L) || steps < 1) return false;
+    batch::Persist2D P;
+    P.L = L;
+    P.u = u;
+    P.slots = slots;
+    P.steps = steps;
+    P.begin = begin;
+    P.C = C;
+    P.Q = Q;
+    P.den = den;
+    P.vel = vel;
+    P.damp = damp;
+    P.W = W;
+    P.zb = batch::ZeroBox2{{zero_box[0], zero_box[1], zero_box[2], zero_box[3]}};
+    P.src = src;
+    P.wavelet = wavelet;
+    P.wavelet_count = wavelet_count;
+    P.dt = dt;
+    P.rec = rec;
+    P.receivers = receivers;
+    for (int e = 0; e < 4; e++) P.bc[e] = bc[e];
+    const int r = L.r;
+    P.tiles_x = (int)((L.nx - 2 * r + 127) / 128);
+    P.tiles_z = (int)((L.nz - 2 * r + 15) / 16);
+    P.ntiles = P.tiles_x * P.tiles_z;
+    // owner-computes sources and edges need r + 1 rows / columns in the first
+    // and last tiles (the first hold min(extent, 16 or 128))
+    const long long last_z = (L.nz - 2 * r) - 16LL * (P.tiles_z - 1);
+    const long long last_x = (L.nx - 2 * r) - 128LL * (P.tiles_x - 1);
+    const long long first_z = std::min<long long>(L.nz - 2 * r, 16);
+    const long long first_x = std::min<long long>(L.nx - 2 * r, 128);
+    P.fused = last_z >= r + 1 && last_x >= r + 1 && first_z >= r + 1 && first_x >= r + 1;
+    P.bar = bar;
+    P.err = err;
+#define SB_P(RR)                                                                    \
+    case RR:                                                                        \
+        return vd ? batch::persistent_r<RR, true>(P, st) : batch::persistent_r<RR, false>(P, st);
+    switch (r) {
+        SB_P(1) SB_P(2) SB_P(3) SB_P(4) SB_P(5) SB_P(6) SB_P(7) SB_P(8) SB_P(9) SB_P(10)
+    }
+#undef SB_P
+    return false;
+}
 
 bool tiled2d_supported(const Layout& L) {
     return L.dim == 2 && L.r >= 1 && L.r <= kMaxRadius && L.pitch % 4 == 0 &&

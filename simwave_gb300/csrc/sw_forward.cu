@@ -336,6 +336,9 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
     return ctx;
 }
 
+// Interior points up to which a 2D float32 run takes the persistent kernel.
+constexpr long long kPersistentPoints = 1500000;
+
 // Frees a run's stream-ordered scratch after its last launch.
 struct ScratchRelease {
     void* p;
@@ -356,6 +359,43 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
     else { phases[0] = 1; phases[1] = 0; nphase = 2; }
     const TiledContext tctx = prepare_tiled<T>(R, st);
     ScratchRelease release{tctx.scratch, st};
+    if constexpr (std::is_same<T, float>::value && DIM == 2) {
+        // small 2D grids: all steps in one persistent launch (the per-step
+        // kernels of such grids are bound by their start-up, not their work)
+        const size_t nsteps = S.steps.size();
+        if (tctx.ok && !ev && !(R.flags & SIMWAVE_FLAG_STEP_LAUNCHES) &&
+            L.interior_points() <= kPersistentPoints && nsteps >= 8 && nsteps < (1u << 28)) {
+            std::vector<int> tab(3 * nsteps + 2, 0);  // slots per step, 2 barrier words
+            for (size_t i = 0; i < nsteps; i++) {
+                tab[3 * i] = S.steps[i].next;
+                tab[3 * i + 1] = S.steps[i].cur;
+                tab[3 * i + 2] = S.steps[i].prev;
+            }
+            void* dtab = nullptr;
+            SW_CUDA(cudaMallocAsync(&dtab, tab.size() * sizeof(int), st));
+            ScratchRelease tab_release{dtab, st};
+            SW_CUDA(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, st));
+            SW_CUDA(cudaStreamSynchronize(st));  // `tab` is host memory of this call
+            for (size_t i = 0; i < nsteps; i++)
+                if (R.before_step) R.before_step(i);
+            int* itab = static_cast<int*>(dtab);
+            if (persistent2d_launch(L, VD, R.u, itab, (int)nsteps, (long long)R.begin,
+                                    tctx.coefC, tctx.coefQ, R.den, R.vel, R.damp, R.W,
+                                    tctx.zero_box, R.src, R.wavelet, R.wavelet_count, R.dt,
+                                    R.rec, R.receivers, R.bc,
+                                    reinterpret_cast<unsigned*>(itab + 3 * nsteps), tctx.err,
+                                    st)) {
+                SW_LAUNCHED("stencil2d_persistent");
+                stats.stencil_variant = 2;
+                stats.stencil_launches += 1;
+                stats.kernel_launches += 1;
+                for (size_t i = 0; i < nsteps; i++)
+                    if (R.after_step) R.after_step(i);
+                return;
+            }
+        }
+    }
     for (size_t i = 0; i < S.steps.size(); i++) {
         const size_t n = R.begin + i;
         T* un = R.u + (size_t)S.steps[i].next * L.slot;

@@ -52,6 +52,20 @@ void tiled2d_launch(const Layout& L, bool vd, float* un, const float* uc, const 
                     const float* C, const float* Q, const float* den,
                     const Weights<float>& W, const int* zero_box, cudaStream_t st);
 
+// Every step of a 2D float32 shot in one cooperative launch (small grids,
+// where per-step kernels are bound by their start-up): `slots` (device) holds
+// the physical next/cur/prev slot of each step, `bar` two zeroed words for
+// the grid barrier, `err` the run's status word. False when the layout or
+// the device does not allow it (nothing launched).
+bool persistent2d_launch(const Layout& L, bool vd, float* u, const int* slots, int steps,
+                         long long begin, const float* C, const float* Q, const float* den,
+                         const float* vel, const float* damp,
+                         const Weights<float>& W, const int* zero_box,
+                         const Windows<float>& src, const float* wavelet,
+                         size_t wavelet_count, float dt, const Windows<float>& rec,
+                         float* receivers, const int* bc, unsigned* bar, int* err,
+                         cudaStream_t st);
+
 // gz = s1_z * sum_k c1_k (rho(z+k) - rho(z-k)) at interior points (3D).
 void form_density_z(const float* den, float* gz, const Layout& L, const Weights<float>& W,
                     cudaStream_t st);

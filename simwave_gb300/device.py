@@ -51,6 +51,7 @@ class Problem(ctypes.Structure):
 FLAG_TIME_KERNELS = 1
 FLAG_WINDOWS_CHECKED = 2
 FLAG_GENERIC_KERNEL = 4
+FLAG_STEP_LAUNCHES = 8
 
 
 def layout(fastest_extent, space_order, precision):
@@ -211,14 +212,16 @@ class DeviceProblem:
         self._u.zero_()
         self.receivers.zero_()
 
-    def run(self, stream=None, time_kernels=False, generic=False):
+    def run(self, stream=None, time_kernels=False, generic=False, step_launches=False):
         """Launch the forward loop on ``stream`` (torch stream or None).
 
-        ``generic`` forces the one-thread-per-point stencil kernel."""
+        ``generic`` forces the one-thread-per-point stencil kernel;
+        ``step_launches`` keeps per-step launches for small 2D grids."""
         lib = _lib.load()
         self.problem.flags = FLAG_WINDOWS_CHECKED | (
             FLAG_TIME_KERNELS if time_kernels else 0) | (
-            FLAG_GENERIC_KERNEL if generic else 0)
+            FLAG_GENERIC_KERNEL if generic else 0) | (
+            FLAG_STEP_LAUNCHES if step_launches else 0)
         handle = None
         if stream is not None:
             handle = ctypes.c_void_p(stream.cuda_stream)

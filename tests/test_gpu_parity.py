@@ -209,10 +209,16 @@ def test_tiled2d_and_generic_kernels_agree(order, vd):
     kw = random_problem(sw, 2, order, vd, bc, 3, shape=(77, 301), tf=0.04,
                         seed=order, nrec=6)
     dp = DeviceProblem(kw)
-    st = dp.run()
+    st = dp.run(step_launches=True)
     dp.status()
     assert st["stencil_variant"] == 1, "tiled 2D kernel not selected"
     tiled_u = dp.u_full_numpy()
+    # the same run with all steps in one persistent launch: same kernels
+    dp.reset()
+    st = dp.run()
+    dp.status()
+    assert st["stencil_variant"] == 2, "persistent 2D launch not selected"
+    assert np.array_equal(dp.u_full_numpy(), tiled_u)
     dp.reset()
     st = dp.run(generic=True)
     assert st["stencil_variant"] == 0
