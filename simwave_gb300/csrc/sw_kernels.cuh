@@ -171,28 +171,31 @@ __global__ void inject_sources(T* __restrict__ un, const T* __restrict__ vel,
 }
 
 // ---- receivers: KWS gather of one receiver window by one warp --------------
-// (constant_density/2d/wave.c:395-464); reads the current level. Lanes take
-// the window's (z[, x]) rows; each row is summed along its contiguous axis;
-// the lane sums are reduced with shuffles. Returns the sum in every lane.
+// (constant_density/2d/wave.c:395-464); reads the current level. Eight lanes
+// run along the window's contiguous axis (y in 3D, x in 2D) and the four
+// lane groups take alternate rows, so one load instruction touches four
+// 32-byte window rows; the lane sums are reduced with shuffles. Returns the
+// sum in every lane.
 template <typename T, int DIM>
 __device__ __forceinline__ T gather_window(const T* uc, const Layout& L, const size_t* b,
                                            const T* v, int lane) {
     const int lz = (int)(b[1] - b[0] + 1), lx = (int)(b[3] - b[2] + 1);
-    const int ly = DIM == 3 ? (int)(b[5] - b[4] + 1) : 1;
+    const int nf = DIM == 3 ? (int)(b[5] - b[4] + 1) : lx;  // contiguous extent
     const int rows = DIM == 3 ? lz * lx : lz;
+    const T* vf = DIM == 3 ? v + lz + lx : v + lz;          // contiguous-axis weights
+    const int sub = lane & 7, grp = lane >> 3;
     T sum = 0;
-    for (int row = lane; row < rows; row += 32) {
-        if (DIM == 3) {
-            const int iz = row / lx, ix = row - iz * lx;
-            const T wzx = v[iz] * v[lz + ix];
-            const T* vy = v + lz + lx;
-            const T* u = uc + L.at3(b[0] + iz, b[2] + ix, b[4]);
-            for (int iy = 0; iy < ly; iy++) sum += u[iy] * (wzx * vy[iy]);
-        } else {
-            const T wz = v[row];
-            const T* vx = v + lz;
-            const T* u = uc + L.at2(b[0] + row, b[2]);
-            for (int ix = 0; ix < lx; ix++) sum += u[ix] * (wz * vx[ix]);
+    for (int f = sub; f - sub < nf; f += 8) {
+        if (f >= nf) continue;
+        const T wf = vf[f];
+        for (int row = grp; row < rows; row += 4) {
+            if (DIM == 3) {
+                const int iz = row / lx, ix = row - iz * lx;
+                const T wzx = v[iz] * v[lz + ix];
+                sum += uc[L.at3(b[0] + iz, b[2] + ix, b[4] + f)] * (wzx * wf);
+            } else {
+                sum += uc[L.at2(b[0] + row, b[2] + f)] * (v[row] * wf);
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
