@@ -13,7 +13,10 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "simwave_gb300.h"
 #include "sw_kernels.cuh"
@@ -562,10 +565,37 @@ static void repack(T* dst, const T* src, const Layout& L, bool to_pitched,
 
 // Page-locks caller arrays for the duration of one call (released by the
 // destructor); ranges already locked by the caller are used as they are.
+// Makes every page of [p, p + bytes) resident, from all host cores, without
+// changing its contents (each page has one byte read and written back).
+// Freshly allocated arrays (numpy.zeros) are mapped lazily; page-locking them
+// would otherwise fault and clear their pages from one thread.
+static void fault_in(void* p, size_t bytes) {
+    if (!p || bytes < ((size_t)64 << 20)) return;
+    const long ps = sysconf(_SC_PAGESIZE);
+    const size_t page = ps > 0 ? (size_t)ps : 4096;
+    const unsigned n = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    char* base = static_cast<char*>(p);
+    const size_t chunk = (bytes / n + page - 1) / page * page;
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < n; t++) {
+        const size_t lo = (size_t)t * chunk;
+        if (lo >= bytes) break;
+        const size_t hi = std::min(bytes, lo + chunk);
+        th.emplace_back([=] {
+            for (size_t o = lo; o < hi; o += page) {
+                volatile char* c = base + o;
+                *c = *c;
+            }
+        });
+    }
+    for (auto& t : th) t.join();
+}
+
 struct HostPins {
     std::vector<void*> mine;
     bool add(const void* p, size_t bytes) {
         if (!p || !bytes) return true;
+        fault_in(const_cast<void*>(p), bytes);
         cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
         if (e == cudaSuccess) {
             mine.push_back(const_cast<void*>(p));
