@@ -78,7 +78,7 @@ def config2_model(n=384):
     return vel, den
 
 
-def config2_arguments(timesteps=None, n=384, stride=50):
+def config2_arguments(timesteps=None, n=384, stride=50, dtype=np.float32):
     """Middleware keyword arguments of the 3D benchmark shot.
 
     ``timesteps`` truncates the run (same dt and wavelet samples) for tests
@@ -88,7 +88,7 @@ def config2_arguments(timesteps=None, n=384, stride=50):
     h = 12.5
     top = (n - 1) * h
     sm = sw.SpaceModel((0, top, 0, top, 0, top), (h, h, h), vel, den,
-                       space_order=8, dtype=np.float32)
+                       space_order=8, dtype=dtype)
     sm.config_boundary(damping_length=40 * h, boundary_condition="none",
                        damping_polynomial_degree=3, damping_alpha=0.001)
     tm = sw.TimeModel(space_model=sm, tf=1.5, saving_stride=stride)
@@ -108,11 +108,10 @@ def config2_arguments(timesteps=None, n=384, stride=50):
         kw["end_timestep"] = T
         kw["wavelet"] = np.ascontiguousarray(kw["wavelet"][:T])
         kw["wavelet_size"] = T
-        kw["shot_record"] = np.zeros((T, kw["num_receivers"]), np.float32)
+        kw["shot_record"] = np.zeros((T, kw["num_receivers"]), dtype)
         nsnap = 1 if stride == 0 else len(range(0, T, stride))
         kw["num_snapshots"] = nsnap + 2
-        kw["u_full"] = np.zeros((nsnap + 2,) + kw["u_full"].shape[1:],
-                                np.float32)
+        kw["u_full"] = np.zeros((nsnap + 2,) + kw["u_full"].shape[1:], dtype)
     return kw
 
 
@@ -130,21 +129,28 @@ def smooth_velocity(shape, rng, lo=1500.0, hi=4500.0, modes=6):
     return (lo + (hi - lo) * f).astype(np.float32)
 
 
-def config3_arguments(nshots=96, seed=7, max_side=2048):
+def config3_arguments(nshots=96, seed=7, max_side=2048, dtype=np.float32, pick=None):
     """The batched workload: 2D constant-density shots with seeded grids of
     256..max_side points per side (10 m), orders {4, 8, 12, 16, 20}, smooth
     random velocity 1500-4500 m/s, 50-point damping layer, an 8-25 Hz Ricker
     source and 256-1024 surface receivers, tf = 1.0 s."""
     import simwave_gb300 as sw
     rng = np.random.default_rng(seed)
-    out = []
+    out, skipped = [], []
     for _ in range(nshots):
         nz, nx = (int(v) for v in rng.integers(256, max_side + 1, size=2))
         order = int(rng.choice([4, 8, 12, 16, 20]))
         h = 10.0
         vel = smooth_velocity((nz, nx), rng)
+        if pick is not None and len(out) + len(skipped) not in pick:
+            # skipped shot: the same draws, so later shots are unchanged
+            skipped.append(None)
+            rng.uniform(0.2, 0.8)
+            rng.integers(256, 1025)
+            rng.uniform(8.0, 25.0)
+            continue
         sm = sw.SpaceModel((0, (nz - 1) * h, 0, (nx - 1) * h), (h, h), vel,
-                           space_order=order, dtype=np.float32)
+                           space_order=order, dtype=dtype)
         sm.config_boundary(damping_length=50 * h, boundary_condition="none",
                            damping_polynomial_degree=3, damping_alpha=0.001)
         tm = sw.TimeModel(space_model=sm, tf=1.0, saving_stride=0)
@@ -207,7 +213,8 @@ def batched_leg(nshots=96, max_side=2048):
             "timing": "CUDA events, resident inputs, setup excluded"}
 
 
-def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320):
+def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320,
+                     dtype=np.float32, pick=None):
     """The served workload: Poisson arrivals (seeded, ``rate`` per second) of
     2D shots (512..max2d per side) and 3D shots (128..max3d per side), orders
     4-16, float32, constant or Gardner density, tf 0.5-2.0 s, 10 m grids,
@@ -237,8 +244,11 @@ def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3
         box = []
         for a in range(len(shape)):
             box += [0.0, (shape[a] - 1) * h]
+        if pick is not None and i not in pick:
+            rng.uniform(8.0, 20.0)  # the skipped request's Ricker draw
+            continue
         sm = sw.SpaceModel(tuple(box), (h,) * len(shape), vel, den, space_order=order,
-                           dtype=np.float32)
+                           dtype=dtype)
         sm.config_boundary(damping_length=30 * h, boundary_condition="none")
         tm = sw.TimeModel(space_model=sm, tf=tf, saving_stride=0)
         mid = [(shape[a] - 1) * h / 2 for a in range(len(shape))]
@@ -301,7 +311,7 @@ def served_leg(nreq=40):
             "speedup_shots_per_s": round(served["shots_per_s"] / seq["shots_per_s"], 2)}
 
 
-def config1_arguments():
+def config1_arguments(dtype=np.float32):
     """The reference README's 2D case: 512^2 model (1500 m/s above row 100,
     2000 below) interpolated onto the 513^2 grid of a 5120 m box at 10 m,
     order 4, no damping layer, boundaries (null_neumann, null_dirichlet,
@@ -311,7 +321,7 @@ def config1_arguments():
     vel = np.full((512, 512), 2000.0, dtype=np.float32)
     vel[:100] = 1500.0
     sm = sw.SpaceModel((0.0, 5120.0, 0.0, 5120.0), (10.0, 10.0), vel, space_order=4,
-                       dtype=np.float32)
+                       dtype=dtype)
     sm.config_boundary(damping_length=0.0, boundary_condition=(
         "null_neumann", "null_dirichlet", "none", "null_dirichlet"))
     tm = sw.TimeModel(space_model=sm, tf=1.0, saving_stride=0)
@@ -392,6 +402,60 @@ def config1_leg(reps=20):
             "hbm_note": "16 B/update algorithmic; the 5 MB state stays in L2"}
 
 
+def accuracy_leg():
+    """Per configuration: the float32 error of the GPU and of the reference's
+    C path (the CPU port, bit-identical to the reference build) against the
+    float64 run (the CPU port in float64 on the same model, built in float64
+    by the front end as the reference's front end does), relative L2 over
+    the shot record and the final wavefield. Config 2 runs its first 51 of
+    1201 steps; configs 3-5 use representative shots."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker of this leg
+    from simwave_gb300.device import DeviceProblem
+
+    def rel(a, b):
+        a = np.asarray(a, np.float64)
+        b = np.asarray(b, np.float64)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    def cpu(kw):
+        k = dict(kw, u_full=np.zeros_like(kw["u_full"]),
+                 shot_record=np.zeros_like(kw["shot_record"]))
+        u, r, _ = oracle.forward("port", x_stride="layout", **k)
+        return u, r
+
+    def gpu(kw):
+        dp = DeviceProblem(kw)
+        dp.run()
+        dp.status()
+        return dp.u_full_numpy(), dp.shot_record_numpy()
+
+    true, smooth = config5_models()
+    _, dt5 = config5_arguments(true, nshots=1)
+    cases = [
+        ("1 plain 2D, 513^2 so4", lambda d: config1_arguments(dtype=d)),
+        ("2 3D VD so8 472^3, steps 1-51", lambda d: config2_arguments(timesteps=51, dtype=d)),
+        ("3 batched shot 3 (1665x1127 so4)", lambda d: config3_arguments(12, pick={3}, dtype=d)[0]),
+        ("3 batched shot 7 (666x1382 so16)", lambda d: config3_arguments(12, pick={7}, dtype=d)[0]),
+        ("4 served 2D Gardner (1330x811 so12)", lambda d: config4_requests(40, pick={0}, dtype=d)[0].kwargs),
+        ("4 served 3D VD (204^3 so8)", lambda d: config4_requests(40, pick={11}, dtype=d)[0].kwargs),
+        ("5 inversion shot 0 forward (459x1809 so8)",
+         lambda d: config5_arguments(smooth, dt=dt5, nshots=1, dtype=d)[0][0]),
+    ]
+    rows = []
+    for name, build in cases:
+        kw32, kw64 = build(np.float32), build(np.float64)
+        u64, r64 = cpu(kw64)
+        u32, r32 = cpu(kw32)
+        gu, gr = gpu(kw32)
+        rows.append({"config": name,
+                     "gpu_f32_vs_f64": {"shot_record": rel(gr, r64), "wavefield": rel(gu, u64)},
+                     "ref_f32_vs_f64": {"shot_record": rel(r32, r64), "wavefield": rel(u32, u64)},
+                     "gpu_vs_ref_f32": {"shot_record": rel(gr, r32), "wavefield": rel(gu, u32)}})
+        print(json.dumps(rows[-1]), flush=True)
+    return rows
+
+
 def config5_models(seed=5):
     """The inversion workload's models on a (351, 1701) grid of 10 m (nz = 351,
     nx = 1701): 12 layers from 1500 to 5500 m/s cut by two dipping faults
@@ -416,7 +480,7 @@ def config5_models(seed=5):
     return true, smooth
 
 
-def config5_arguments(vel, dt=None, nshots=16, damping_points=50):
+def config5_arguments(vel, dt=None, nshots=16, damping_points=50, dtype=np.float32):
     """Middleware keyword arguments of the inversion shots on ``vel``: so 8,
     8 Hz Ricker, tf 3.0 s, sources at 20 m depth spread over x, 1701
     receivers at 10 m depth (one per grid column), a 50-point damping layer
@@ -426,7 +490,7 @@ def config5_arguments(vel, dt=None, nshots=16, damping_points=50):
     nz, nx = vel.shape
     h = 10.0
     sm = sw.SpaceModel((0.0, (nz - 1) * h, 0.0, (nx - 1) * h), (h, h), vel,
-                       space_order=8, dtype=np.float32)
+                       space_order=8, dtype=dtype)
     sm.config_boundary(damping_length=damping_points * h, boundary_condition="none",
                        damping_polynomial_degree=3, damping_alpha=0.001)
     tm = sw.TimeModel(space_model=sm, tf=3.0, dt=dt, saving_stride=0)
@@ -680,6 +744,8 @@ def main():
                     help="run only the served (continuous batching) leg")
     ap.add_argument("--gradient", action="store_true",
                     help="run only the inversion (velocity gradient) leg")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="run only the float32-vs-float64 error table (CPU-heavy)")
     ap.add_argument("--no-served", action="store_true",
                     help="skip the served leg of the default line")
     ap.add_argument("--no-gradient", action="store_true",
@@ -688,6 +754,11 @@ def main():
 
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+
+    if args.accuracy:
+        print(json.dumps({"metric": "float32 error vs the float64 run, per config",
+                          "rows": accuracy_leg()}), flush=True)
         return
 
     if args.gradient:

@@ -161,3 +161,29 @@ def test_full_size_stride_invariance(big_problem):
     torch.cuda.synchronize()
     assert torch.equal(dp4.u[nsnap], last0)
     assert torch.equal(dp4.receivers, rec0)
+
+
+def test_config1_float32_error_matches_reference():
+    """The reference README's 2D case (513^2, order 4, T 328, both boundary
+    phases): the GPU's float32 error against the float64 run is the
+    reference float32 path's own error to within a factor of two."""
+    import bench
+    import oracle
+    from simwave_gb300.device import DeviceProblem
+
+    def cpu(kw):
+        k = dict(kw, u_full=np.zeros_like(kw["u_full"]),
+                 shot_record=np.zeros_like(kw["shot_record"]))
+        u, r, _ = oracle.forward("port", **k)
+        return u, r
+
+    kw32, kw64 = bench.config1_arguments(np.float32), bench.config1_arguments(np.float64)
+    u64, r64 = cpu(kw64)
+    u32, r32 = cpu(kw32)
+    dp = DeviceProblem(kw32)
+    dp.run()
+    dp.status()
+    gu, gr = dp.u_full_numpy(), dp.shot_record_numpy()
+    for g, ref, exact in ((gr, r32, r64), (gu, u32, u64)):
+        assert rel_l2(g, exact) <= 2.0 * rel_l2(ref, exact)
+        assert rel_l2(g, ref) <= 1e-4
