@@ -161,6 +161,10 @@ struct Buffer {
         if (n == 0) return nullptr;
         SW_CUDA(cudaMalloc(&ptr, n));
         SW_CUDA(cudaMemset(ptr, 0, n));  // row padding is never written
+        // the memset runs on the legacy stream, which the library's
+        // non-blocking streams do not wait for: finish it before any copy
+        // into the buffer can be queued
+        SW_CUDA(cudaDeviceSynchronize());
         bytes = n;
         return ptr;
     }
@@ -283,6 +287,7 @@ static int* device_words() {
     if (!w) {
         SW_CUDA(cudaMalloc(&w, 16 * sizeof(int)));
         SW_CUDA(cudaMemset(w, 0, 16 * sizeof(int)));
+        SW_CUDA(cudaDeviceSynchronize());  // zeroed before any stream reads it
     }
     return w;
 }
