@@ -266,6 +266,28 @@ def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3
     return reqs
 
 
+def warm_arguments(dim, order, vd, big=False):
+    """A short shot (tf 0.03 s) of the given class on a 48^2 / 32^3 model, or
+    on a 1300^2 one (`big`: past the persistent-launch size of 2D runs), to
+    load its kernels before timing (CUDA loads a kernel's code at its first
+    launch)."""
+    import simwave_gb300 as sw
+    n, h = ((1300 if big else 48), 10.0) if dim == 2 else (32, 10.0)
+    shape = (n,) * dim
+    vel = np.full(shape, 2000.0, dtype=np.float32)
+    den = np.full(shape, 1000.0, dtype=np.float32) if vd else None
+    box = []
+    for _ in range(dim):
+        box += [0.0, (n - 1) * h]
+    sm = sw.SpaceModel(tuple(box), (h,) * dim, vel, den, space_order=order, dtype=np.float32)
+    sm.config_boundary(damping_length=5 * h, boundary_condition="none")
+    tm = sw.TimeModel(space_model=sm, tf=0.03, saving_stride=0)
+    mid = [(n - 1) * h / 2] * dim
+    src = sw.Source(sm, coordinates=[mid], window_radius=4)
+    rec = sw.Receiver(sm, coordinates=[mid], window_radius=4)
+    return sw.Solver(sm, tm, src, rec, sw.RickerWavelet(15.0, tm)).forward_arguments()
+
+
 def served_leg(nreq=40):
     """p50/p99 latency and shots/s of the continuous-batching server against
     the same requests run one after another through the drop-in host path."""
@@ -273,10 +295,22 @@ def served_leg(nreq=40):
     import io
     import torch
     from simwave_gb300.backend.middleware import Middleware
-    from simwave_gb300.serve import ShotServer, latency_summary
+    from simwave_gb300.serve import Request, ShotServer, latency_summary
     reqs = config4_requests(nreq)
     arrivals = [r.arrival for r in reqs]
     updates = sum(interior_updates(r.kwargs)[1] for r in reqs)
+    # load every kernel class of the workload on both paths first
+    classes = sorted({(r.kwargs["velocity_model"].ndim, int(r.kwargs["space_order"]),
+                       r.kwargs.get("density_model") is not None) for r in reqs})
+    warm = [warm_arguments(*c) for c in classes]
+    warm += [warm_arguments(*c, big=True) for c in classes if c[0] == 2]
+    with contextlib.redirect_stdout(io.StringIO()):
+        for kw in warm:
+            Middleware().exec("forward", **dict(kw, u_full=np.zeros_like(kw["u_full"]),
+                                                shot_record=np.zeros_like(kw["shot_record"])))
+    warm_server = ShotServer(epoch_steps=64)
+    warm_server.serve([Request(kw, 0.0) for kw in warm])
+    warm_server.close()
     # sequential: Solver.forward's host path, one request at a time
     mw = Middleware()
     service = []

@@ -1163,15 +1163,28 @@ void launch_vecp_any(float* un, const float* uc, const float* up, const float* c
         launch_vecp<R, VD, MINB, false>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
 }
 
+// The kernel AUTO runs for radius r (measured on a 408^3 grid, ms per
+// launch): the packed kernel for r <= 4 (constant density at order 2 keeps
+// the float4 kernel: 0.224 vs 0.265); for r = 5..8 the packed kernel where
+// it beat the scalar one (constant density: 0.31/0.29/0.41 vs
+// 0.37/0.45/0.46 at orders 10/12/14, the one-CTA build at order 16: 0.47 vs
+// 0.51; variable density only at order 10: 0.52 vs 0.63, its register
+// spills lose above), else the scalar kernel.
+int auto_policy(int r, bool vd) {
+    if (r <= 4) return (!vd && r == 1) ? SIMWAVE_POLICY_VEC_2CTA : SIMWAVE_POLICY_VEC_PACKED;
+    if (r <= 8) {
+        if (vd) return r == 5 ? SIMWAVE_POLICY_VEC_PACKED : SIMWAVE_POLICY_SCALAR_TILED;
+        return r == 8 ? SIMWAVE_POLICY_VEC_PACKED_1CTA : SIMWAVE_POLICY_VEC_PACKED;
+    }
+    return SIMWAVE_POLICY_SCALAR_TILED;
+}
+
 template <int R, bool VD>
 void launch_vec_policy(int policy, float* un, const float* uc, const float* up,
                        const float* coefC, const float* den, const float* coefQ,
                        const Layout& L, const Weights<float>& W, const TiledContext& ctx,
                        cudaStream_t st) {
-    // AUTO: the packed kernel, except constant density at order 2 where the
-    // plain float4 kernel measured faster (0.224 vs 0.265 ms, 408^3 grid)
-    if (policy == SIMWAVE_POLICY_AUTO)
-        policy = (!VD && R == 1) ? SIMWAVE_POLICY_VEC_2CTA : SIMWAVE_POLICY_VEC_PACKED;
+    if (policy == SIMWAVE_POLICY_AUTO) policy = auto_policy(R, VD);
     switch (policy) {
         case SIMWAVE_POLICY_VEC_2CTA:
             return launch_vec<R, VD, 2, false, false>(un, uc, up, coefC, den, coefQ, L, W, ctx, st);
@@ -1197,10 +1210,10 @@ void form_density_z(const float* den, float* gz, const Layout& L, const Weights<
 }
 
 bool wants_density_z(const Layout& L, bool vd) {
-    const int p = kernel_policy();
-    return vd && L.dim == 3 && L.r <= 4 &&
-           (p == SIMWAVE_POLICY_AUTO || p == SIMWAVE_POLICY_VEC_PACKED ||
-            p == SIMWAVE_POLICY_VEC_PACKED_1CTA);
+    int p = kernel_policy();
+    if (p == SIMWAVE_POLICY_AUTO) p = auto_policy(L.r, vd);
+    return vd && L.dim == 3 && L.r <= 8 &&
+           (p == SIMWAVE_POLICY_VEC_PACKED || p == SIMWAVE_POLICY_VEC_PACKED_1CTA);
 }
 
 void form_coefficients(const float* vel, const float* damp, float* C, float* Q,
@@ -1245,7 +1258,7 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
     std::memcpy(ctx.map_rho, &mr, sizeof(mr));
     // float4 kernel: orders up to 8, 16-byte aligned rows and arrays
     ctx.vec = false;
-    if (r <= 4 && (L.lead + r) % 4 == 0) {
+    if (r <= 8 && (L.lead + r) % 4 == 0) {
         const int vw = 128 + 2 * round4(r), vh = kWarps + 2 * r;
         CUtensorMap vu, vr;
         if (encode_map(&vu, u_base, L, nslots, slot_stride, vw, vh) &&
@@ -1266,6 +1279,27 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, 
                   const float* vel, const float* den, const float* damp, const Layout& L,
                   const Weights<float>& W, float dt, float dt2, cudaStream_t st) {
     const int policy = kernel_policy();
+    const bool aligned =
+        (reinterpret_cast<uintptr_t>(vel) | reinterpret_cast<uintptr_t>(damp) |
+         reinterpret_cast<uintptr_t>(un) | reinterpret_cast<uintptr_t>(up) |
+         reinterpret_cast<uintptr_t>(uc)) % 16 == 0;
+    const int high = (policy == SIMWAVE_POLICY_AUTO && L.r >= 5) ? auto_policy(L.r, vd) : policy;
+    if (ctx.vec && L.r >= 5 && L.r <= 8 && aligned &&
+        (high == SIMWAVE_POLICY_VEC_PACKED || high == SIMWAVE_POLICY_VEC_PACKED_1CTA)) {
+        const bool one = high == SIMWAVE_POLICY_VEC_PACKED_1CTA;
+#define SW_VECH(RR)                                                                           \
+    case RR:                                                                                  \
+        if (vd) {                                                                             \
+            if (one) launch_vecp_any<RR, true, 1>(un, uc, up, vel, den, damp, L, W, ctx, st);  \
+            else launch_vecp_any<RR, true, 2>(un, uc, up, vel, den, damp, L, W, ctx, st);      \
+        } else {                                                                              \
+            if (one) launch_vecp_any<RR, false, 1>(un, uc, up, vel, den, damp, L, W, ctx, st); \
+            else launch_vecp_any<RR, false, 2>(un, uc, up, vel, den, damp, L, W, ctx, st);     \
+        }                                                                                     \
+        return;
+        switch (L.r) { SW_VECH(5) SW_VECH(6) SW_VECH(7) SW_VECH(8) }
+#undef SW_VECH
+    }
     if (ctx.vec && L.r <= 4 && policy != SIMWAVE_POLICY_SCALAR_TILED &&
         (reinterpret_cast<uintptr_t>(vel) | reinterpret_cast<uintptr_t>(damp) |
          reinterpret_cast<uintptr_t>(un) | reinterpret_cast<uintptr_t>(up) |
