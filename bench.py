@@ -174,9 +174,11 @@ def batched_leg(nshots=96, max_side=2048):
     probs = [DeviceProblem(k) for k in kws]
     updates = sum(interior_updates(k)[1] for k in kws)
     stream = torch.cuda.current_stream()
-    # plain: one simwave_forward_device call per shot, back to back
-    probs[0].run()
-    probs[0].status()
+    # plain: one simwave_forward_device call per shot, back to back (every
+    # shot once untimed first, so no kernel is loaded inside the timing)
+    for p in probs:
+        p.run()
+    probs[-1].status()
     for p in probs:
         p.reset()
     torch.cuda.synchronize()
