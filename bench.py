@@ -914,7 +914,7 @@ def main():
     if rank == 0 and not args.no_served:
         served = leg(served_leg)
     if rank == 0 and not args.no_gradient:
-        gradient = leg(gradient_leg, steps=1)
+        gradient = leg(gradient_leg, steps=2)  # best of two
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
