@@ -9,6 +9,7 @@
 #include <chrono>
 #include <functional>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -690,6 +691,15 @@ static double host_forward(const HostArgs<T>& A) {
     // the copy engines move them with pitched DMA (AUTO), or let kernels
     // address the pageable arrays directly (DIRECT, coherent host links), or
     // one contiguous copy per grid through device staging (STAGED)
+    // SIMWAVE_TRACE set: phase times of this call on stderr
+    const bool trace = std::getenv("SIMWAVE_TRACE") != nullptr;
+    auto stamp = [&](const char* what) {
+        if (trace)
+            std::fprintf(stderr, "simwave host entry: %-14s %9.3f ms\n", what,
+                         1e3 * std::chrono::duration<double>(
+                                   std::chrono::steady_clock::now() - t0).count());
+    };
+    stamp("checked");
     HostPins pins;
     bool pinned = false;
     if (g_transfer_mode == SIMWAVE_TRANSFER_AUTO) {
@@ -697,6 +707,7 @@ static double host_forward(const HostArgs<T>& A) {
                  pins.add(A.damp, dense_bytes) && (!A.vd || pins.add(A.den, dense_bytes));
         if (!pinned) pins.release();
     }
+    stamp("pinned");
     const bool direct = !pinned && ar.host_access && g_transfer_mode == SIMWAVE_TRANSFER_DIRECT;
     T* sin[2] = {nullptr, nullptr};
     T* sout[2] = {nullptr, nullptr};
@@ -820,7 +831,9 @@ static double host_forward(const HostArgs<T>& A) {
     R.after_step = [&](size_t i) {
         for (int p : done_at[i]) emit(p);
     };
+    stamp("uploads queued");
     dispatch_steps<T>(R, S, st, stats, nullptr);
+    stamp("steps queued");
 
     // slots that changed identity without being written
     for (size_t p = 0; p < A.nslots; p++)
@@ -838,6 +851,9 @@ static double host_forward(const HostArgs<T>& A) {
     SW_CUDA(cudaStreamSynchronize(st));
     SW_CUDA(cudaStreamSynchronize(cin));
     SW_CUDA(cudaStreamSynchronize(cout));
+    stamp("all done");
+    pins.release();
+    stamp("unpinned");
     check_device_words(st);
     const double secs =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

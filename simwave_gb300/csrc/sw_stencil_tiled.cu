@@ -1029,9 +1029,13 @@ void launch_r(float* un, const float* uc, const float* up, const float* vel, con
     const int ty = (int)((L.ny - 2 * R + 31) / 32);
     const int tx = (int)((L.nx - 2 * R + TL::TX - 1) / TL::TX);
     const int nzi = (int)(L.nz - 2 * R);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stencil3d_tiled<R, VD>, kThreads,
-                                                  smem);
+    static int per_sm_of[64] = {};  // resident CTAs per SM, queried once per device
+    if (!per_sm_of[dev & 63]) {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stencil3d_tiled<R, VD>, kThreads, smem);
+        per_sm_of[dev & 63] = std::max(v, 1);
+    }
+    const int per_sm = per_sm_of[dev & 63];
     const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
@@ -1107,8 +1111,13 @@ void launch_vec(float* un, const float* uc, const float* up, const float* coefC,
     const int ty = (int)((L.ny - 2 * R + 127) / 128);
     const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
     const int nzi = (int)(L.nz - 2 * R);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    static int per_sm_of[64] = {};  // resident CTAs per SM, queried once per device
+    if (!per_sm_of[dev & 63]) {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, kThreads, smem);
+        per_sm_of[dev & 63] = std::max(v, 1);
+    }
+    const int per_sm = per_sm_of[dev & 63];
     const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
@@ -1137,8 +1146,13 @@ void launch_vecp(float* un, const float* uc, const float* up, const float* coefC
     const int ty = (int)((L.ny - 2 * R + 127) / 128);
     const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
     const int nzi = (int)(L.nz - 2 * R);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    static int per_sm_of[64] = {};  // resident CTAs per SM, queried once per device
+    if (!per_sm_of[dev & 63]) {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, kThreads, smem);
+        per_sm_of[dev & 63] = std::max(v, 1);
+    }
+    const int per_sm = per_sm_of[dev & 63];
     const int chunk = choose_chunk(ty, tx, nzi, R, per_sm);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
