@@ -241,6 +241,23 @@ class DeviceProblem:
         if status != 0:
             raise RuntimeError("device status {}: {}".format(status, _lib.last_error()))
 
+    def grid_view(self, flat):
+        """The logical ``(nz, nx[, ny])`` view of one pitched grid buffer
+        (``slot`` elements)."""
+        return self._view(flat, None)
+
+    @property
+    def wavefield_bytes(self):
+        """Device bytes of the wavefield slots (0 once released)."""
+        return 0 if self._u is None else self._u.numel() * self._u.element_size()
+
+    def release_wavefield(self):
+        """Drop the device wavefield slots; returns the bytes freed."""
+        freed = self.wavefield_bytes
+        self._u = None
+        self.u = None
+        return freed
+
     def release_inputs(self):
         """Drop the device copies of the models and tables; the wavefield
         slots and the shot record stay."""

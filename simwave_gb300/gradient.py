@@ -39,7 +39,7 @@ class _ShotRecord(torch.autograd.Function):
                 tuple(velocity.shape), tuple(problem.shape)))
         lib = _lib.load()
         p = problem.problem
-        problem._view(problem.vel, None).copy_(velocity.detach())
+        problem.grid_view(problem.vel).copy_(velocity.detach())
         grids = ctypes.c_size_t()
         _check(lib.simwave_gradient_checkpoints(ctypes.byref(p), ctypes.c_size_t(interval),
                                                 ctypes.byref(grids)), "checkpoint count")
@@ -68,7 +68,7 @@ class _ShotRecord(torch.autograd.Function):
             ctypes.c_void_p(ck.data_ptr()), ctypes.c_void_p(g.data_ptr()),
             ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
             "simwave_gradient_backward")
-        return problem._view(out, None).contiguous(), None, None
+        return problem.grid_view(out).contiguous(), None, None
 
 
 def shot_record(velocity, problem, interval=None):

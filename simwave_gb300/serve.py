@@ -191,10 +191,8 @@ class ShotServer:
         for req in self.done:
             if self.in_use + need <= self.budget:
                 return
-            if req.problem is not None and req.problem._u is not None and not req.evicted:
-                freed = req.problem._u.numel() * req.problem._u.element_size()
-                req.problem._u = None
-                req.problem.u = None
+            if req.problem is not None and req.problem.wavefield_bytes and not req.evicted:
+                freed = req.problem.release_wavefield()
                 req.evicted = True
                 self.in_use -= freed
                 self.resident -= freed
@@ -204,7 +202,7 @@ class ShotServer:
         req.shot_record = req.problem.shot_record_numpy()
         req.completed = time.perf_counter()
         # the wavefield slots stay resident; models and tables are dropped
-        resident = req.problem._u.numel() * req.problem._u.element_size()
+        resident = req.problem.wavefield_bytes
         req.problem.release_inputs()
         self.in_use -= req.bytes - resident
         self.resident += resident
