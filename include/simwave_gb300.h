@@ -347,7 +347,9 @@ typedef struct simwave_stats {
     size_t kernel_launches;   /* all kernel launches of this library */
     size_t h2d_bytes, d2h_bytes;
     int stencil_variant;      /* 0 generic, 1 tiled, 2 tiled 2D, all steps
-                                 in one persistent launch */
+                                 in one persistent launch, 3 tiled 2D, each
+                                 step (stencil, sources, boundaries,
+                                 receivers) in one launch */
 } simwave_stats;
 
 /* No reference counterpart (the reference returns only its wall time). */

@@ -782,25 +782,11 @@ static int guarded(F&& f) {
 // spins with a time limit: on expiry the block records SIMWAVE_E_TIMEOUT and
 // the kernel ends (blocks still inside a barrier time out the same way).
 
-struct Persist2D {
-    Layout L;
+struct Persist2D : Shot2D {
     float* u;                 // slot 0
     const int* slots;         // per step: next, cur, prev physical slots
     int steps;
     long long begin;
-    const float *C, *Q, *den;
-    const float *vel, *damp;  // source scaling, as the per-step path forms it
-    Weights<float> W;
-    ZeroBox2 zb;
-    Windows<float> src;
-    const float* wavelet;
-    size_t wavelet_count;
-    float dt;
-    Windows<float> rec;
-    float* receivers;
-    int bc[4];
-    int tiles_x, tiles_z, ntiles;
-    int fused;                // sources and edges by the owning tile (see below)
     unsigned* bar;            // [0] arrivals, [1] generation (zeroed before launch)
     int* err;
 };
@@ -809,9 +795,10 @@ struct Persist2D {
 // source points in the tile (points of the halo belong to the nearest edge
 // tile), then the x edges of its rows if it is an x-edge tile, then the z
 // edges of its columns if it is a z-edge tile. Exact when the first and last
-// tiles hold at least r + 1 rows and columns: every boundary operation then
-// reads and writes points of one tile only, in the reference's order.
-__device__ void tile_sources_edges(const Persist2D& P, float* un, long long n, int tz, int tx) {
+// tiles hold at least r + 1 rows and columns (Shot2D::fused): every boundary
+// operation then reads and writes points of one tile only, in the
+// reference's order.
+__device__ void tile_sources_edges(const Shot2D& P, float* un, long long n, int tz, int tx) {
     const Layout& L = P.L;
     const int r = L.r;
     const int nz = (int)L.nz, nx = (int)L.nx;
@@ -912,7 +899,7 @@ stencil2d_persistent(const Persist2D P) {
         const float* up = P.u + (long long)P.slots[3 * i + 2] * L.slot;
         // stencil tiles, then the receivers (they read u_cur only)
         for (int t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
-            stencil2d_tile<R, VD, TZ>(tile, L, un, uc, up, P.C, P.Q, P.den, P.W, P.zb.b,
+            stencil2d_tile<R, VD, TZ>(tile, L, un, uc, up, P.C, P.Q, P.den, P.W, P.zb,
                                       t / P.tiles_x, t % P.tiles_x);
             __syncthreads();  // the tile buffer is restaged next
             if (P.fused) tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x);
@@ -950,6 +937,45 @@ stencil2d_persistent(const Persist2D P) {
     }
 }
 
+// One time step of a 2D shot in one launch: blocks [0, ntiles) compute a
+// tile each (stencil, then the sources and boundary edges the tile owns),
+// the blocks after them gather the receivers (they read u_cur only).
+template <int R, bool VD, int TZ>
+__global__ void __launch_bounds__(kThreads)
+stencil2d_step(const Shot2D P, float* un, const float* uc, const float* up, long long n) {
+    if ((int)blockIdx.x < P.ntiles) {
+        const int t = blockIdx.x;
+        stencil2d_tile<R, VD, TZ>(reinterpret_cast<float*>(sw_batch_smem), P.L, un, uc, up, P.C,
+                                  P.Q, P.den, P.W, P.zb, t / P.tiles_x, t % P.tiles_x);
+        __syncthreads();
+        tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x);
+        return;
+    }
+    const long long w = ((long long)(blockIdx.x - P.ntiles) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (long long)P.rec.count) return;
+    const float sum = gather_window<float, 2>(uc, P.L, P.rec.interval + w * 4,
+                                              P.rec.values + P.rec.offsets[w], threadIdx.x & 31);
+    if ((threadIdx.x & 31) == 0) P.receivers[(n - 1) * (long long)P.rec.count + w] = sum;
+}
+
+template <int R, bool VD>
+static void step_r(const Shot2D& P, float* un, const float* uc, const float* up, long long n,
+                   cudaStream_t st) {
+    constexpr int TZ = 16;
+    constexpr int HX = (R + 3) & ~3;
+    const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
+    static bool configured[64] = {};
+    int dev = 0;
+    SB_CUDA(cudaGetDevice(&dev));
+    if (!configured[dev & 63]) {
+        SB_CUDA(cudaFuncSetAttribute(stencil2d_step<R, VD, TZ>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        configured[dev & 63] = true;
+    }
+    const int rec_blocks = (int)((P.rec.count + kWarps - 1) / kWarps);
+    stencil2d_step<R, VD, TZ><<<P.ntiles + rec_blocks, kThreads, bytes, st>>>(P, un, uc, up, n);
+}
+
 template <int R, bool VD>
 static bool persistent_r(const Persist2D& P, cudaStream_t st) {
     constexpr int TZ = 16;
@@ -980,52 +1006,69 @@ static bool persistent_r(const Persist2D& P, cudaStream_t st) {
 
 }  // namespace batch
 
-bool persistent2d_launch(const Layout& L, bool vd, float* u, const int* slots, int steps,
-                         long long begin, const float* C, const float* Q, const float* den,
-                         const float* vel, const float* damp,
-                         const Weights<float>& W, const int* zero_box,
-                         const Windows<float>& src, const float* wavelet,
-                         size_t wavelet_count, float dt, const Windows<float>& rec,
-                         float* receivers, const int* bc, unsigned* bar, int* err,
-                         cudaStream_t st) {
-    if (!tiled2d_supported(L) || steps < 1) return false;
+bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
+                    const float* den, const float* vel, const float* damp,
+                    const Weights<float>& W, const int* zero_box, const Windows<float>& src,
+                    const float* wavelet, size_t wavelet_count, float dt,
+                    const Windows<float>& rec, float* receivers, const int* bc) {
+    if (!tiled2d_supported(L)) return false;
+    S.L = L;
+    S.C = C;
+    S.Q = Q;
+    S.den = den;
+    S.vel = vel;
+    S.damp = damp;
+    S.W = W;
+    for (int i = 0; i < 4; i++) S.zb[i] = zero_box[i];
+    S.src = src;
+    S.wavelet = wavelet;
+    S.wavelet_count = wavelet_count;
+    S.dt = dt;
+    S.rec = rec;
+    S.receivers = receivers;
+    for (int e = 0; e < 4; e++) S.bc[e] = bc[e];
+    const int r = L.r;
+    S.tiles_x = (int)((L.nx - 2 * r + 127) / 128);
+    S.tiles_z = (int)((L.nz - 2 * r + 15) / 16);
+    S.ntiles = S.tiles_x * S.tiles_z;
+    // owner-computes sources and edges need r + 1 rows / columns in the first
+    // and last tiles (the first hold min(extent, 16 or 128))
+    const long long last_z = (L.nz - 2 * r) - 16LL * (S.tiles_z - 1);
+    const long long last_x = (L.nx - 2 * r) - 128LL * (S.tiles_x - 1);
+    const long long first_z = std::min<long long>(L.nz - 2 * r, 16);
+    const long long first_x = std::min<long long>(L.nx - 2 * r, 128);
+    S.fused = last_z >= r + 1 && last_x >= r + 1 && first_z >= r + 1 && first_x >= r + 1;
+    return true;
+}
+
+void step2d_launch(const Shot2D& S, bool vd, float* un, const float* uc, const float* up,
+                   long long n, cudaStream_t st) {
+#define SB_ST(RR)                                                               \
+    case RR:                                                                    \
+        if (vd) batch::step_r<RR, true>(S, un, uc, up, n, st);                  \
+        else batch::step_r<RR, false>(S, un, uc, up, n, st);                    \
+        break;
+    switch (S.L.r) {
+        SB_ST(1) SB_ST(2) SB_ST(3) SB_ST(4) SB_ST(5) SB_ST(6) SB_ST(7) SB_ST(8) SB_ST(9) SB_ST(10)
+    }
+#undef SB_ST
+}
+
+bool persistent2d_launch(const Shot2D& S, bool vd, float* u, const int* slots, int steps,
+                         long long begin, unsigned* bar, int* err, cudaStream_t st) {
+    if (steps < 1) return false;
     batch::Persist2D P;
-    P.L = L;
+    static_cast<Shot2D&>(P) = S;
     P.u = u;
     P.slots = slots;
     P.steps = steps;
     P.begin = begin;
-    P.C = C;
-    P.Q = Q;
-    P.den = den;
-    P.vel = vel;
-    P.damp = damp;
-    P.W = W;
-    P.zb = batch::ZeroBox2{{zero_box[0], zero_box[1], zero_box[2], zero_box[3]}};
-    P.src = src;
-    P.wavelet = wavelet;
-    P.wavelet_count = wavelet_count;
-    P.dt = dt;
-    P.rec = rec;
-    P.receivers = receivers;
-    for (int e = 0; e < 4; e++) P.bc[e] = bc[e];
-    const int r = L.r;
-    P.tiles_x = (int)((L.nx - 2 * r + 127) / 128);
-    P.tiles_z = (int)((L.nz - 2 * r + 15) / 16);
-    P.ntiles = P.tiles_x * P.tiles_z;
-    // owner-computes sources and edges need r + 1 rows / columns in the first
-    // and last tiles (the first hold min(extent, 16 or 128))
-    const long long last_z = (L.nz - 2 * r) - 16LL * (P.tiles_z - 1);
-    const long long last_x = (L.nx - 2 * r) - 128LL * (P.tiles_x - 1);
-    const long long first_z = std::min<long long>(L.nz - 2 * r, 16);
-    const long long first_x = std::min<long long>(L.nx - 2 * r, 128);
-    P.fused = last_z >= r + 1 && last_x >= r + 1 && first_z >= r + 1 && first_x >= r + 1;
     P.bar = bar;
     P.err = err;
 #define SB_P(RR)                                                                    \
     case RR:                                                                        \
         return vd ? batch::persistent_r<RR, true>(P, st) : batch::persistent_r<RR, false>(P, st);
-    switch (r) {
+    switch (S.L.r) {
         SB_P(1) SB_P(2) SB_P(3) SB_P(4) SB_P(5) SB_P(6) SB_P(7) SB_P(8) SB_P(9) SB_P(10)
     }
 #undef SB_P

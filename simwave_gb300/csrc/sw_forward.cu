@@ -368,6 +368,18 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
     else { phases[0] = 1; phases[1] = 0; nphase = 2; }
     const TiledContext tctx = prepare_tiled<T>(R, st);
     ScratchRelease release{tctx.scratch, st};
+    // 2D float32 tiled runs: the step parameters of the owner-computes
+    // kernels (sources and boundary edges applied by the tile that holds
+    // them, right after its stencil)
+    Shot2D shot{};
+    bool fused2d = false;
+    if constexpr (std::is_same<T, float>::value && DIM == 2) {
+        if (tctx.ok)
+            fused2d = shot2d_prepare(shot, L, tctx.coefC, tctx.coefQ, R.den, R.vel, R.damp, R.W,
+                                     tctx.zero_box, R.src, R.wavelet, R.wavelet_count, R.dt,
+                                     R.rec, R.receivers, R.bc) &&
+                      shot.fused && !ev;
+    }
     if constexpr (std::is_same<T, float>::value && DIM == 2) {
         // small 2D grids: all steps in one persistent launch (the per-step
         // kernels of such grids are bound by their start-up, not their work)
@@ -389,10 +401,8 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
             for (size_t i = 0; i < nsteps; i++)
                 if (R.before_step) R.before_step(i);
             int* itab = static_cast<int*>(dtab);
-            if (persistent2d_launch(L, VD, R.u, itab, (int)nsteps, (long long)R.begin,
-                                    tctx.coefC, tctx.coefQ, R.den, R.vel, R.damp, R.W,
-                                    tctx.zero_box, R.src, R.wavelet, R.wavelet_count, R.dt,
-                                    R.rec, R.receivers, R.bc,
+            if (shot.L.dim == 2 &&
+                persistent2d_launch(shot, VD, R.u, itab, (int)nsteps, (long long)R.begin,
                                     reinterpret_cast<unsigned*>(itab + 3 * nsteps), tctx.err,
                                     st)) {
                 SW_LAUNCHED("stencil2d_persistent");
@@ -411,6 +421,17 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
         const T* uc = R.u + (size_t)S.steps[i].cur * L.slot;
         const T* up = R.u + (size_t)S.steps[i].prev * L.slot;
         if (R.before_step) R.before_step(i);
+        if constexpr (std::is_same<T, float>::value && DIM == 2) {
+            if (fused2d) {  // the whole step in one launch
+                step2d_launch(shot, VD, un, uc, up, (long long)n, st);
+                SW_LAUNCHED("stencil2d_step");
+                stats.stencil_variant = 3;
+                stats.stencil_launches++;
+                stats.kernel_launches++;
+                if (R.after_step) R.after_step(i);
+                continue;
+            }
+        }
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i], st));
         launch_stencil<T, DIM, VD>(R, tctx, un, uc, up, st, &stats.stencil_variant);
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i + 1], st));

@@ -221,6 +221,11 @@ struct Ctx {
     bool tiled = false;
     long long grid = 0;  // elements of one grid (nz * pitch)
     bool dirichlet = false;
+    float* receivers = nullptr;
+    // one launch per step (tiled, owner-computes sources and edges): with
+    // the receiver record, and without it (recomputed segments)
+    bool fused = false;
+    Shot2D shot{}, shot_quiet{};
 };
 
 // Checks the problem and copies the windows to the host (`src_iv`, ...).
@@ -328,6 +333,7 @@ static Ctx make_ctx(const simwave_problem* P, cudaStream_t st, HostWindows* rec_
                            P->rec_points_values_offset, P->num_receivers};
     X.begin = P->begin_timestep;
     X.end = P->end_timestep;
+    X.receivers = (float*)P->receivers;
     return X;
 }
 
@@ -347,6 +353,16 @@ static void prepare_coefficients(Ctx& X, Scratch& mem, bool aligned) {
     GR_CUDA(cudaStreamSynchronize(mem.st));
     const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
     for (int i = 0; i < 6; i++) X.zero_box[i] = good ? box[i] : 0;
+    // Dirichlet runs save the boundary lines between the sources and the
+    // boundary conditions of each step: those keep separate launches
+    if (X.dirichlet) return;
+    X.fused = shot2d_prepare(X.shot, X.L, X.C, X.Q, nullptr, X.vel, X.damp, X.W, X.zero_box,
+                             X.src, X.wavelet, X.wavelet_count, X.dt, X.rec, X.receivers,
+                             X.bc) &&
+              X.shot.fused;
+    X.shot_quiet = X.shot;
+    X.shot_quiet.rec.count = 0;
+    if (!X.receivers) X.shot.rec.count = 0;
 }
 
 // The forward stencil on (un, uc, up): the tiled kernel on C and Q, else the
@@ -371,6 +387,12 @@ static void stencil(const Ctx& X, float* un, const float* uc, const float* up,
 // `ring_row`, the record of u^n into `rec_row` (either may be null).
 static void forward_step(const Ctx& X, float* un, const float* uc, const float* up,
                          size_t n, float* ring_row, float* rec_row, cudaStream_t st) {
+    if (X.fused && !ring_row) {
+        // the record goes to X.receivers + (n - 1) * count, where rec_row points
+        step2d_launch(rec_row ? X.shot : X.shot_quiet, false, un, uc, up, (long long)n, st);
+        GR_LAUNCHED("stencil2d_step");
+        return;
+    }
     stencil(X, un, uc, up, st);
     if (X.src.count) {
         inject_sources<float, 2><<<(unsigned)X.src.count, 128, 0, st>>>(

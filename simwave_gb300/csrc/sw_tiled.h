@@ -52,19 +52,46 @@ void tiled2d_launch(const Layout& L, bool vd, float* un, const float* uc, const 
                     const float* C, const float* Q, const float* den,
                     const Weights<float>& W, const int* zero_box, cudaStream_t st);
 
-// Every step of a 2D float32 shot in one cooperative launch (small grids,
-// where per-step kernels are bound by their start-up): `slots` (device) holds
-// the physical next/cur/prev slot of each step, `bar` two zeroed words for
-// the grid barrier, `err` the run's status word. False when the layout or
-// the device does not allow it (nothing launched).
-bool persistent2d_launch(const Layout& L, bool vd, float* u, const int* slots, int steps,
-                         long long begin, const float* C, const float* Q, const float* den,
-                         const float* vel, const float* damp,
-                         const Weights<float>& W, const int* zero_box,
-                         const Windows<float>& src, const float* wavelet,
-                         size_t wavelet_count, float dt, const Windows<float>& rec,
-                         float* receivers, const int* bc, unsigned* bar, int* err,
-                         cudaStream_t st);
+// A 2D float32 shot's step parameters for the tiled stencil with
+// owner-computes sources and boundary edges (sw_batch.cu): tiles of 16 x 128
+// interior points; `fused` is set when the first and last tiles hold at
+// least r + 1 rows and columns (then each tile can apply the sources and the
+// boundary operations of its own points after its stencil, exactly).
+struct Shot2D {
+    Layout L;
+    const float *C, *Q, *den, *vel, *damp;
+    Weights<float> W;
+    int zb[4];
+    Windows<float> src;
+    const float* wavelet;
+    size_t wavelet_count;
+    float dt;
+    Windows<float> rec;
+    float* receivers;
+    int bc[4];
+    int tiles_x, tiles_z, ntiles;
+    int fused;
+};
+
+// Fills `S`; false when the layout does not suit the tiled 2D kernel.
+bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
+                    const float* den, const float* vel, const float* damp,
+                    const Weights<float>& W, const int* zero_box, const Windows<float>& src,
+                    const float* wavelet, size_t wavelet_count, float dt,
+                    const Windows<float>& rec, float* receivers, const int* bc);
+
+// Step n of `S` (fused only) in one launch: stencil, sources, edges and the
+// record of u_cur.
+void step2d_launch(const Shot2D& S, bool vd, float* un, const float* uc, const float* up,
+                   long long n, cudaStream_t st);
+
+// Every step of `S` in one cooperative launch (small grids, where per-step
+// kernels are bound by their start-up): `slots` (device) holds the physical
+// next/cur/prev slot of each step, `bar` two zeroed words for the grid
+// barrier, `err` the run's status word. False when the device does not
+// allow it (nothing launched).
+bool persistent2d_launch(const Shot2D& S, bool vd, float* u, const int* slots, int steps,
+                         long long begin, unsigned* bar, int* err, cudaStream_t st);
 
 // gz = s1_z * sum_k c1_k (rho(z+k) - rho(z-k)) at interior points (3D).
 void form_density_z(const float* den, float* gz, const Layout& L, const Weights<float>& W,

@@ -209,16 +209,20 @@ def test_tiled2d_and_generic_kernels_agree(order, vd):
     kw = random_problem(sw, 2, order, vd, bc, 3, shape=(77, 301), tf=0.04,
                         seed=order, nrec=6)
     dp = DeviceProblem(kw)
-    st = dp.run(step_launches=True)
+    # separate stencil, source, boundary and receiver kernels per step
+    st = dp.run(time_kernels=True)
     dp.status()
     assert st["stencil_variant"] == 1, "tiled 2D kernel not selected"
-    tiled_u = dp.u_full_numpy()
-    # the same run with all steps in one persistent launch: same kernels
-    dp.reset()
-    st = dp.run()
-    dp.status()
-    assert st["stencil_variant"] == 2, "persistent 2D launch not selected"
-    assert np.array_equal(dp.u_full_numpy(), tiled_u)
+    tiled_u, tiled_rec = dp.u_full_numpy(), dp.shot_record_numpy()
+    # one launch per step (owner-computes sources and edges where the edge
+    # tiles are wide enough), then all steps in one persistent launch
+    for flags, variants in (({"step_launches": True}, (1, 3)), ({}, (2,))):
+        dp.reset()
+        st = dp.run(**flags)
+        dp.status()
+        assert st["stencil_variant"] in variants, st["stencil_variant"]
+        assert np.array_equal(dp.u_full_numpy(), tiled_u)
+        assert np.array_equal(dp.shot_record_numpy(), tiled_rec)
     dp.reset()
     st = dp.run(generic=True)
     assert st["stencil_variant"] == 0
@@ -226,3 +230,20 @@ def test_tiled2d_and_generic_kernels_agree(order, vd):
     ru, rrec = port_forward(kw)
     assert_close(tiled_u, ru, np.float32, "tiled 2D wavefield")
     assert rel_l2(tiled_u, gen_u) < 2e-5
+
+
+@pytest.mark.parametrize("order,vd", [(2, False), (4, True), (8, False), (12, True)])
+def test_fused_step_sources_across_tiles(order, vd):
+    """One launch per step with many wide source windows that straddle tile
+    borders and the damping layer, against the checker."""
+    from simwave_gb300.device import DeviceProblem
+    bc = ("null_dirichlet", "null_neumann", "null_neumann", "null_dirichlet")
+    kw = random_problem(sw, 2, order, vd, bc, 0, shape=(126, 290), tf=0.05, seed=order,
+                        nsrc=9, nrec=7, src_radius=10, rec_radius=10, multi=True)
+    dp = DeviceProblem(kw)
+    st = dp.run(step_launches=True)
+    dp.status()
+    assert st["stencil_variant"] == 3, "fused step kernel not selected"
+    ru, rrec = port_forward(kw)
+    assert_close(dp.u_full_numpy(), ru, np.float32, "fused-step wavefield")
+    assert_close(dp.shot_record_numpy(), rrec, np.float32, "fused-step shot record")
