@@ -189,11 +189,11 @@ def batched_leg(nshots=96, max_side=2048):
     e1.record(stream)
     e1.synchronize()
     plain_s = e0.elapsed_time(e1) / 1e3
-    # batch: tile heights picked per order, then one engine for all shots
-    tiles = autotune(probs, steps=32)
+    # batch: tile height and time-blocking depth picked per order, then one
+    # engine for all shots
+    tiles = autotune(probs)
     eng = BatchEngine()
-    for order, rows in tiles.items():
-        eng.set_tile_rows(order, rows)
+    eng.apply(tiles)
     for p in probs:
         p.reset()
     torch.cuda.synchronize()
@@ -211,7 +211,7 @@ def batched_leg(nshots=96, max_side=2048):
             "speedup_vs_plain": round(plain_s / batch_s, 2),
             "batch_gpts": round(updates / batch_s / 1e9, 2),
             "plain_gpts": round(updates / plain_s / 1e9, 2),
-            "tile_rows": tiles, "batch_launches": int(launches),
+            "tuning": {str(k): v for k, v in tiles.items()}, "batch_launches": int(launches),
             "timing": "CUDA events, resident inputs, setup excluded"}
 
 

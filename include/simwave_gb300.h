@@ -331,10 +331,25 @@ int simwave_batch_run(simwave_batch *batch, int steps, void *stream);
 /* Time steps left for a shot (0 when finished). */
 int simwave_batch_remaining(simwave_batch *batch, int shot_id, int *steps);
 /* Remove a shot; a finished shot's slots are put back in the reference's
- * order first. Waits for the batch's work. */
+ * order first. Waits for the batch's work. An unfinished shot leaves its
+ * latest two levels in the schedule's current slots (a later call can
+ * resume from there); with time blocking, the third rotating slot may hold
+ * an older level than the per-step kernels would have left in it. */
 int simwave_batch_release(simwave_batch *batch, int shot_id);
 /* Tuning: stencil tile height (8, 16 or 32 rows) for one space order. */
 int simwave_batch_set_tile_rows(simwave_batch *batch, int space_order, int rows);
+/* Tuning: time-blocking depth for one space order -- 1 (default: a launch
+ * per step), or 2..4 steps per launch where depth x space_order / 2 <= 32
+ * (and the tile keeps >= 64 owned columns). A tile stages 96 rows of
+ * u_cur and u_prev once and advances them `depth` steps in shared memory
+ * (sources, boundary conditions and receiver records included), trading
+ * recomputed tile margins for fewer passes over HBM. Shots with variable
+ * density, a source window reaching into the halo, or a receiver window
+ * wider than a tile keep depth 1; results equal depth 1's within float32
+ * rounding (receiver sums are added per tile). */
+int simwave_batch_set_depth(simwave_batch *batch, int space_order, int depth);
+/* Depth a shot runs at under the current settings. */
+int simwave_batch_depth(simwave_batch *batch, int shot_id, int *depth);
 /* Kernel launches enqueued so far (graph nodes counted per replay). */
 int simwave_batch_launches(simwave_batch *batch, size_t *launches);
 

@@ -1,10 +1,13 @@
 """Many 2D shots advanced together (``simwave_batch_*`` of the C library).
 
 ``BatchEngine`` keeps device-resident shots (``DeviceProblem``) and advances
-all unfinished ones together: one stencil launch per (order, density) group
-and one launch per sparse term per time step, captured as a CUDA graph of 16
-steps and replayed. ``run_batch`` runs a list of problems to completion;
-``autotune`` picks the stencil tile height per order by timing.
+all unfinished ones together: one stencil launch per (order, density, depth)
+group and one launch per sparse term per time step, captured as a CUDA graph
+of 16 launches per group and replayed. With a time-blocking depth k > 1 for
+an order, each launch advances that order's constant-density shots k steps
+(sources, boundaries and receiver records inside the kernel). ``run_batch``
+runs a list of problems to completion; ``autotune`` picks the tile height and
+the depth per order by timing.
 """
 import ctypes
 import time
@@ -15,6 +18,7 @@ from .backend import _lib
 from .device import DeviceProblem
 
 TILE_ROWS = (8, 16, 32)
+DEPTHS = (2, 3, 4)
 
 
 def _check(status):
@@ -45,10 +49,17 @@ class BatchEngine:
         except Exception:
             pass
 
-    def add(self, problem):
-        """Admit a ``DeviceProblem``; returns its shot id."""
+    def add(self, problem, ready=None):
+        """Admit a ``DeviceProblem``; returns its shot id. The engine reads
+        the problem's arrays on its own stream at once, so this waits for
+        ``ready`` (the event its uploads complete at) or, without one, for
+        the current stream."""
         if not isinstance(problem, DeviceProblem):
             raise TypeError("expected a DeviceProblem")
+        if ready is not None:
+            ready.synchronize()
+        else:
+            torch.cuda.current_stream(problem.device).synchronize()
         sid = ctypes.c_int()
         _check(self._lib.simwave_batch_add(self._h, ctypes.byref(problem.problem),
                                            ctypes.byref(sid)))
@@ -75,6 +86,24 @@ class BatchEngine:
     def set_tile_rows(self, space_order, rows):
         _check(self._lib.simwave_batch_set_tile_rows(self._h, ctypes.c_int(space_order),
                                                      ctypes.c_int(rows)))
+
+    def set_depth(self, space_order, depth):
+        """Time-blocking depth (steps per launch) for one space order."""
+        _check(self._lib.simwave_batch_set_depth(self._h, ctypes.c_int(space_order),
+                                                 ctypes.c_int(depth)))
+
+    def depth(self, shot_id):
+        """Steps per launch the shot runs at under the current settings."""
+        out = ctypes.c_int()
+        _check(self._lib.simwave_batch_depth(self._h, ctypes.c_int(shot_id),
+                                             ctypes.byref(out)))
+        return out.value
+
+    def apply(self, tuning):
+        """Settings from ``autotune``: ``{order: {"rows": r, "depth": k}}``."""
+        for order, t in tuning.items():
+            self.set_tile_rows(int(order), int(t["rows"]))
+            self.set_depth(int(order), int(t["depth"]))
 
     def launches(self):
         out = ctypes.c_size_t()
@@ -104,28 +133,47 @@ def run_batch(problems, engine=None, chunk=256):
     return problems
 
 
-def autotune(problems, steps=32, rows=TILE_ROWS):
-    """Pick the stencil tile height per space order by timing ``steps`` steps
-    of the given shots with every candidate; returns ``{order: rows}``."""
+def _candidates(order, rows, depths, device):
+    """(rows, depth) settings the library accepts for ``order``."""
+    out = [(r, 1) for r in rows]
+    probe = BatchEngine(device)
+    try:
+        for k in depths:
+            try:
+                probe.set_depth(order, k)
+            except RuntimeError:
+                continue
+            out.append((16, k))
+    finally:
+        probe.close()
+    return out
+
+
+def autotune(problems, steps=64, rows=TILE_ROWS, depths=DEPTHS):
+    """Pick the tile height and the time-blocking depth per space order by
+    timing ``steps`` steps of the given shots with every candidate; returns
+    ``{order: {"rows": r, "depth": k}}`` (``BatchEngine.apply`` takes it)."""
     orders = sorted({int(p.problem.space_order) for p in problems})
     best = {}
     for order in orders:
         group = [p for p in problems if int(p.problem.space_order) == order]
         timings = {}
-        for r in rows:
+        for r, k in _candidates(order, rows, depths, group[0].device):
             eng = BatchEngine(group[0].device)
             eng.set_tile_rows(order, r)
+            eng.set_depth(order, k)
             for p in group:
                 p.reset()
                 eng.add(p)
-            eng.run(16)  # warm-up (graph capture)
+            eng.run(steps)  # warm-up (graph capture, kernel load)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             eng.run(steps)
             torch.cuda.synchronize()
-            timings[r] = time.perf_counter() - t0
+            timings[(r, k)] = time.perf_counter() - t0
             eng.close()
-        best[order] = min(timings, key=timings.get)
+        r, k = min(timings, key=timings.get)
+        best[order] = {"rows": r, "depth": k}
     for p in problems:
         p.reset()
     return best

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -56,6 +57,19 @@ struct Shot {
     const int* slots;      // [end - begin + 1][3]: physical prev, cur, next
     float dt, dt2;
     int n, begin, end;     // next step to run, first and last step
+    int stop;              // last step of the current run (<= end)
+    int depth;             // steps per launch: 1 per-step kernels, > 1 time-blocked
+    const unsigned char* keep;  // per step: its level is the last one written to its slot
+    float* partial;        // time-blocked receivers: [rec][depth][win] window values
+    int win;               // floats per receiver window in `partial`
+    int halo_zero;         // every slot's halo is zero (no reloads needed)
+    // time-blocked shots carry their latest two levels in two engine-owned
+    // pairs of grids, [pair][prev, cur] (`grid` floats each): a launch
+    // stages from pair *pairp and leaves its last two levels in the other,
+    // so no tile reads a grid another tile of the launch writes
+    float* ext;
+    int* pairp;
+    long long grid;
     int bc[4];
     int zb[4];             // z0, z1, x0, x1: box where Q is zero
 };
@@ -66,12 +80,57 @@ struct ZeroBox2 {
 
 struct TileRef {
     int shot, tz, tx;
+    int rec_first, rec_count;  // time-blocked tiles: their (receiver, slot) entries
 };
 struct PairRef {
     int shot, item;
 };
 
-__device__ __forceinline__ bool active(const Shot& s) { return s.n <= s.end; }
+__device__ __forceinline__ bool active(const Shot& s) { return s.n <= s.stop; }
+
+// ---- time-blocked tiles ----------------------------------------------------------
+// A time-blocked CTA owns OZ x OX interior points (plus the halo beyond them
+// on the grid's edges) and stages a region of kTbRows rows around them: K R
+// rows above and below, and 128 computed columns plus an HX halo, of which
+// DX on each side are recomputed margin. After step k of the block the
+// region's rows are exact k R rows further in and its computed columns
+// (k - 1) R columns further in, so after K steps the owned points are.
+constexpr int kTbRows = 96;
+
+struct TbGeom {
+    int mz, oz, dx, ox;
+};
+
+// Part of one receiver window inside one time-blocked tile's owned points.
+struct TbRec {
+    int rc;              // receiver
+    int z0, z1, x0, x1;  // the part (grid indices, half-open)
+    int b0, b2, lx;      // window origin and row length
+};
+
+__host__ __device__ constexpr TbGeom tb_geom(int r, int k) {
+    // the staged HX columns beyond the 128 computed ones serve the first
+    // step only, so k - 1 further steps eat (k - 1) r computed columns a side
+    const int dx = ((k - 1) * r + 3) & ~3;
+    return TbGeom{k * r, kTbRows - 2 * k * r, dx, 128 - 2 * dx};
+}
+
+__host__ __device__ constexpr bool tb_supported(int r, int k) {
+    const TbGeom g = tb_geom(r, k);
+    return k >= 2 && k <= 4 && g.oz >= 32 && g.ox >= 64;
+}
+
+__host__ __device__ __forceinline__ int tb_tiles(long long interior, int o) {
+    return (int)((interior + o - 1) / o);
+}
+
+// Owned tile along an axis of n points (radius r, o owned points a tile).
+__host__ __device__ __forceinline__ int tb_tile_of(long long p, int r, long long n, int o) {
+    const int t = tb_tiles(n - 2 * r, o);
+    if (p < r) return 0;
+    const long long q = (p - r) / o;
+    return (int)(q < t - 1 ? q : t - 1);
+}
 
 __device__ __forceinline__ void slot_ptrs(const Shot& s, float*& un, const float*& uc,
                                           const float*& up) {
@@ -260,6 +319,395 @@ stencil2d_batched(const Shot* __restrict__ shots, const TileRef* __restrict__ ti
                               S.Q, S.den, S.W, S.zb, t.tz, t.tx);
 }
 
+// ---- time-blocked 2D stencil (constant density) -----------------------------------
+// Copies the owned points [zlo, zhi) x [xlo, xhi) of a staged buffer (row
+// pitch tw, region origin zr0, xc0) to the same points of grid g.
+__device__ __forceinline__ void tb_copy_owned(const float* buf, float* g, int tw, int zr0,
+                                              int xc0, int zlo, int zhi, int xlo, int xhi,
+                                              int pitch, int lead, int warp, int lane) {
+    const int xa = xlo - ((lead + xlo) & 3);  // 16-byte aligned start
+    const int nch = (xhi - xa + 3) / 4;
+    for (int zz = zlo + warp; zz < zhi; zz += kWarps) {
+        const float* srow = buf + (zz - zr0) * tw - xc0;
+        float* grow = g + (long long)zz * pitch + lead;
+        for (int c = lane; c < nch; c += 32) {
+            const int x4 = xa + 4 * c;
+            if (x4 >= xlo && x4 + 3 < xhi) {
+                *reinterpret_cast<float4*>(grow + x4) = *reinterpret_cast<const float4*>(srow + x4);
+            } else {
+                for (int v = 0; v < 4; v++)
+                    if (x4 + v >= xlo && x4 + v < xhi) grow[x4 + v] = srow[x4 + v];
+            }
+        }
+    }
+}
+
+// One CTA advances its tile K steps: u_cur and u_prev of the region are staged
+// in shared memory once, then each step computes u_next in place of u_prev
+// (each point's own previous value is the only one read there) and the two
+// buffers swap roles. Per step, in the order of the per-step kernels: the
+// stencil on the region's rows still exact after this step, the halo points
+// of the new level as its slot holds them (skipped when every slot's halo is
+// zero), the sources, x edges, z edges. The owned points of each receiver
+// window are copied from each level before it is advanced (the sums are
+// formed afterwards, in the per-step kernels' order). A level goes back to
+// its slot only when it is one of the last two of the block (the next block
+// starts from them) or the last write to its slot (snapshots, final slots).
+template <int R, int K>
+__global__ void __launch_bounds__(kThreads, 2)
+stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ tiles,
+                 const TbRec* __restrict__ trec) {
+    constexpr int HX = (R + 3) & ~3;
+    constexpr int TW = 128 + 2 * HX;
+    constexpr int TH = kTbRows;
+    constexpr int NC = (4 + 2 * HX) / 4;
+    constexpr TbGeom G = tb_geom(R, K);
+    constexpr int MZ = G.mz, OZ = G.oz, DX = G.dx, OX = G.ox;
+    static_assert(tb_supported(R, K), "time-block depth too large for the radius");
+    const TileRef t = tiles[blockIdx.x];
+    const Shot& S = shots[t.shot];
+    if (S.n > S.stop) return;
+    const int n0 = S.n;
+    const int kk = min(K, S.stop - n0 + 1);
+    const Layout L = S.L;
+    const int nz = (int)L.nz, nx = (int)L.nx, pitch = (int)L.pitch, lead = (int)L.lead;
+    const int tiles_z = tb_tiles(nz - 2 * R, OZ), tiles_x = tb_tiles(nx - 2 * R, OX);
+    const int zr0 = R + t.tz * OZ - MZ;  // grid row of region row 0
+    const int xr0 = R + t.tx * OX - DX;  // first computed column
+    const int xc0 = xr0 - HX;            // grid column of region column 0
+    const int zlo = t.tz == 0 ? 0 : R + t.tz * OZ;
+    const int zhi = t.tz == tiles_z - 1 ? nz : R + (t.tz + 1) * OZ;
+    const int xlo = t.tx == 0 ? 0 : R + t.tx * OX;
+    const int xhi = t.tx == tiles_x - 1 ? nx : R + (t.tx + 1) * OX;
+    float* U = reinterpret_cast<float*>(sw_batch_smem);
+    float* P = U + TH * TW;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int pair = *S.pairp;
+    {
+        const float* up = S.ext + (long long)(2 * pair) * S.grid;
+        const float* uc = up + S.grid;
+        constexpr int CH = TW / 4;
+#pragma unroll 4
+        for (int i = threadIdx.x; i < TH * CH; i += kThreads) {
+            const int row = i / CH, ch = i - row * CH;
+            const int z = zr0 + row;
+            const int col = lead + xc0 + 4 * ch;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+            if (z >= 0 && z < nz && col >= 0 && col + 3 < pitch) {
+                const long long p = (long long)z * pitch + col;
+                a = *reinterpret_cast<const float4*>(uc + p);
+                b = *reinterpret_cast<const float4*>(up + p);
+            }
+            *reinterpret_cast<float4*>(U + row * TW + 4 * ch) = a;
+            *reinterpret_cast<float4*>(P + row * TW + 4 * ch) = b;
+        }
+    }
+    P2 w2[R + 1];
+#pragma unroll
+    for (int k = 0; k <= R; k++) w2[k] = pk(S.W.c2[k], S.W.c2[k]);
+    const P2 ihx = pk(S.W.ih2[1], S.W.ih2[1]), ihz = pk(S.W.ih2[0], S.W.ih2[0]);
+    const P2 one = pk(1.f, 1.f);
+    const int x = xr0 + 4 * lane;  // this lane's first column
+    const bool xbox = x >= S.zb[2] && x + 3 < S.zb[3];
+    const bool xany = x + 3 >= R && x < nx - R && lead + x >= 0;
+    const bool xfull = x >= R && x + 3 < nx - R;
+    // the region holds an edge line or halo points of the grid
+    const bool edge = zr0 <= R || zr0 + TH > nz - R - 1 || xc0 <= R || xc0 + TW > nx - R - 1;
+    const bool reload = edge && !S.halo_zero;
+    const int bz0 = S.bc[0], bz1 = S.bc[1], bx0 = S.bc[2], bx1 = S.bc[3];
+    __syncthreads();
+    if (kk == 1)  // the block's last two levels: the staged u_cur and the one it computes
+        tb_copy_owned(U, S.ext + (long long)(2 * (pair ^ 1)) * S.grid, TW, zr0, xc0, zlo, zhi,
+                      xlo, xhi, pitch, lead, warp, lane);
+    for (int j = 0; j < kk; j++) {
+        const int n = n0 + j;
+        // receivers: this tile's part of each window of level n, to scratch
+        for (int e = warp; e < t.rec_count; e += kWarps) {
+            const TbRec q = trec[t.rec_first + e];
+            const int w = q.x1 - q.x0;
+            const int cnt = (q.z1 - q.z0) * w;
+            float* dst = S.partial + ((size_t)q.rc * K + j) * S.win;
+            for (int i = lane; i < cnt; i += 32) {
+                const int z = q.z0 + i / w, xx = q.x0 + i % w;
+                dst[(z - q.b0) * q.lx + (xx - q.b2)] = U[(z - zr0) * TW + (xx - xc0)];
+            }
+        }
+        // stencil over the rows that stay exact after this step; each warp
+        // requests its next row's coefficients before computing this one
+        const int rlo = (j + 1) * R, rhi = TH - (j + 1) * R;
+        int rr = rlo + warp;
+        V4 cc_n = {{0ull}, {0ull}}, qq_n = {{0ull}, {0ull}};
+        bool qz_n = true;
+        auto fetch = [&](int row) {
+            const int z = zr0 + row;
+            const bool ok = row < rhi && z >= R && z < nz - R && xany;
+            const long long p = (long long)z * pitch + lead + x;
+            qz_n = xbox && z >= S.zb[0] && z < S.zb[1];
+            cc_n = ldg_v4(S.C + p, ok);
+            qq_n = ldg_v4(S.Q + p, ok && !qz_n);
+        };
+        fetch(rr);
+        for (; rr < rhi; rr += kWarps) {
+            const V4 cc = cc_n, qq = qq_n;
+            const bool qzero = qz_n;
+            fetch(rr + kWarps);
+            const int z = zr0 + rr;
+            if (z < R || z >= nz - R || !xany) continue;
+            const float* tu = U + rr * TW + 4 * lane;
+            const V4 u0 = lds_v4(tu + HX);
+            V4 sz = vmul(w2[0], u0);
+#pragma unroll
+            for (int k = 1; k <= R; k++) {
+                const V4 a = lds_v4(tu + k * TW + HX);
+                const V4 b = lds_v4(tu - k * TW + HX);
+                sz = vfma(w2[k], vadd(a, b), sz);
+            }
+            V4 sx;
+            {
+                P2 ev[2 * NC], od[2 * NC - 1];
+                YWindow<NC>::load(tu, ev, od);
+                P2 sh[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    sh[h] = mul2(w2[0], h ? u0.hi : u0.lo);
+#pragma unroll
+                    for (int k = 1; k <= R; k++) {
+                        const P2 a = YWindow<NC>::at(ev, od, HX + 2 * h + k);
+                        const P2 b = YWindow<NC>::at(ev, od, HX + 2 * h - k);
+                        sh[h] = fma2(w2[k], add2(a, b), sh[h]);
+                    }
+                }
+                sx = {sh[0], sh[1]};
+            }
+            const V4 lap = vfma(ihz, sz, vmul(ihx, sx));
+            float* dst = P + rr * TW + HX + 4 * lane;
+            const V4 pv = lds_v4(dst);
+            V4 av = {fma2(sub2(qq.lo, one), pv.lo, add2(u0.lo, u0.lo)),
+                     fma2(sub2(qq.hi, one), pv.hi, add2(u0.hi, u0.hi))};
+            if (!qzero) {
+                const float4 q4 = to_f4(qq);
+                const V4 rq = from_f4(make_float4(rcp_approx(1.f + q4.x), rcp_approx(1.f + q4.y),
+                                                  rcp_approx(1.f + q4.z), rcp_approx(1.f + q4.w)));
+                av = {mul2(av.lo, rq.lo), mul2(av.hi, rq.hi)};
+            }
+            const V4 out = {fma2(lap.lo, cc.lo, av.lo), fma2(lap.hi, cc.hi, av.hi)};
+            if (xfull) {
+                sts_v4(dst, out);
+            } else {
+                const float4 o = to_f4(out);
+                const float oa[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    if (x + v >= R && x + v < nx - R) dst[v] = oa[v];
+            }
+        }
+        __syncthreads();
+        float* un = S.u + (long long)S.slots[3 * (n - S.begin) + 2] * L.slot;
+        if (reload) {
+            // halo points of the new level: what its slot holds (the per-step
+            // kernels never write them before the boundary phases); halo rows
+            // of the region first, then the halo columns of its interior rows
+            const int ra = max(zr0, 0), rb = min(zr0 + TH, nz);
+            const int ca = max(xc0, 0), cb = min(xc0 + TW, nx);
+            const int w = max(0, cb - ca);
+            const int top = max(0, min(R, rb) - ra);
+            const int bot0 = max(nz - R, ra), bot = max(0, rb - bot0);
+            const int m0 = max(ra, R), m1 = min(rb, nz - R), nm = max(0, m1 - m0);
+            const int nl = max(0, min(R, cb) - ca), right0 = max(nx - R, ca);
+            const int nr = max(0, cb - right0), per = nl + nr;
+            const int A = (top + bot) * w, B = nm * per;
+#pragma unroll 4
+            for (int i = threadIdx.x; i < A + B; i += kThreads) {
+                int zz, xx;
+                if (i < A) {
+                    const int row = i / w;
+                    zz = row < top ? ra + row : bot0 + (row - top);
+                    xx = ca + (i - row * w);
+                } else {
+                    const int k = i - A, row = k / per, c = k - row * per;
+                    zz = m0 + row;
+                    xx = c < nl ? ca + c : right0 + (c - nl);
+                }
+                P[(zz - zr0) * TW + (xx - xc0)] = un[L.at2(zz, xx)];
+            }
+            __syncthreads();
+        }
+        if (S.src.count) {
+            const float dt2 = S.dt2;
+            for (size_t s = 0; s < S.src.count; s++) {
+                const float w = wavelet_at(S.wavelet, (size_t)S.wavelet_count, (size_t)n,
+                                           S.src.count, s);
+                if (w == 0.f) continue;
+                const size_t* b = S.src.interval + 4 * s;
+                if ((int)b[1] < zr0 || (int)b[0] >= zr0 + TH || (int)b[3] < xc0 ||
+                    (int)b[2] >= xc0 + TW)
+                    continue;
+                const float* v = S.src.values + S.src.offsets[s];
+                const long long total = window_size<2>(b);
+                for (long long q = threadIdx.x; q < total; q += kThreads) {
+                    long long iz, ix, iy;
+                    window_point<2>(b, q, iz, ix, iy);
+                    const int z = (int)(b[0] + iz), xx = (int)(b[2] + ix);
+                    if (z < zr0 || z >= zr0 + TH || xx < xc0 || xx >= xc0 + TW) continue;
+                    const float kws = window_weight<float, 2>(b, v, iz, ix, iy);
+                    const long long p = L.at2(z, xx);
+                    const float vv = S.vel[p] * S.vel[p];
+                    const float d = 1.f + S.damp[p] * S.dt * vv * 0.5f;
+                    atomicAdd(P + (z - zr0) * TW + (xx - xc0), dt2 * vv * kws * w / d);
+                }
+            }
+            __syncthreads();
+        }
+        if (edge) {
+            // x edges on the interior rows, then z edges on the interior columns
+            const int r0 = max(zr0, R), r1 = min(zr0 + TH, nz - R);
+            const bool left = bx0 && R >= xc0 && R < xc0 + TW;
+            const bool right = bx1 && nx - R - 1 >= xc0 && nx - R - 1 < xc0 + TW;
+            if (left || right) {
+                for (int i = r0 + threadIdx.x; i < r1; i += kThreads) {
+                    float* row = P + (i - zr0) * TW - xc0;  // indexed by grid column
+                    if (left) {
+                        if (bx0 == 1) row[R] = 0.f;
+                        else
+                            for (int q = 1; q <= R; q++)
+                                if (R - q >= xc0) row[R - q] = row[R + q];
+                    }
+                    if (right) {
+                        const int e = nx - R - 1;
+                        if (bx1 == 1) row[e] = 0.f;
+                        else
+                            for (int q = 1; q <= R; q++)
+                                if (e + q < xc0 + TW) row[e + q] = row[e - q];
+                    }
+                }
+            }
+            __syncthreads();
+            const int c0 = max(xc0, R), c1 = min(xc0 + TW, nx - R);
+            const bool top = bz0 && R >= zr0 && R < zr0 + TH;
+            const bool bottom = bz1 && nz - R - 1 >= zr0 && nz - R - 1 < zr0 + TH;
+            if (top || bottom) {
+                for (int c = c0 + threadIdx.x; c < c1; c += kThreads) {
+                    float* col = P + (c - xc0) - zr0 * TW;  // indexed by grid row * TW
+                    if (top) {
+                        if (bz0 == 1) col[R * TW] = 0.f;
+                        else
+                            for (int q = 1; q <= R; q++)
+                                if (R - q >= zr0) col[(R - q) * TW] = col[(R + q) * TW];
+                    }
+                    if (bottom) {
+                        const int e = nz - R - 1;
+                        if (bz1 == 1) col[e * TW] = 0.f;
+                        else
+                            for (int q = 1; q <= R; q++)
+                                if (e + q < zr0 + TH) col[(e + q) * TW] = col[(e - q) * TW];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // owned points of the level: every one to the other pair when it is
+        // one of the block's last two; to its slot, as the per-step kernels
+        // write it (interior and Neumann mirrors), when that is the slot's
+        // last write
+        if (j >= kk - 2)
+            tb_copy_owned(P, S.ext + (long long)(2 * (pair ^ 1) + (j - (kk - 2))) * S.grid, TW,
+                          zr0, xc0, zlo, zhi, xlo, xhi, pitch, lead, warp, lane);
+        if (S.keep[n - S.begin]) {
+            const int xa = xlo - ((lead + xlo) & 3);  // 16-byte aligned start
+            const int nch = (xhi - xa + 3) / 4;
+            for (int zz = zlo + warp; zz < zhi; zz += kWarps) {
+                const bool zin = zz >= R && zz < nz - R;
+                const float* srow = P + (zz - zr0) * TW - xc0;
+                float* grow = un + (long long)zz * pitch + lead;
+                for (int c = lane; c < nch; c += 32) {
+                    const int x4 = xa + 4 * c;
+                    if (zin && x4 >= max(xlo, R) && x4 + 3 < min(xhi, nx - R)) {
+                        *reinterpret_cast<float4*>(grow + x4) =
+                            *reinterpret_cast<const float4*>(srow + x4);
+                        continue;
+                    }
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const int xx = x4 + v;
+                        if (xx < xlo || xx >= xhi) continue;
+                        const bool xin = xx >= R && xx < nx - R;
+                        bool st = zin && xin;
+                        if (!st && zin != xin)  // halo of one axis: Neumann mirrors only
+                            st = xin ? S.bc[zz < R ? 0 : 1] == 2 : S.bc[xx < R ? 2 : 3] == 2;
+                        if (st) grow[xx] = srow[xx];
+                    }
+                }
+            }
+        }
+        float* tmp = U;
+        U = P;
+        P = tmp;
+    }
+}
+
+// Receiver records of the time-blocked shots from the window copies: one
+// warp per receiver, each level summed in the per-step gather's order (the
+// records equal the per-step kernels' bit for bit).
+__global__ void receivers_tblock(const Shot* __restrict__ shots,
+                                 const PairRef* __restrict__ pairs, int npairs) {
+    const int wid = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (wid >= npairs) return;
+    const PairRef pr = pairs[wid];
+    const Shot& S = shots[pr.shot];
+    if (!active(S)) return;
+    const int K = S.depth;
+    const int kk = min(K, S.stop - S.n + 1);
+    const size_t* b = S.rec.interval + 4 * (size_t)pr.item;
+    const float* v = S.rec.values + S.rec.offsets[pr.item];
+    const int lz = (int)(b[1] - b[0] + 1), lx = (int)(b[3] - b[2] + 1);
+    const float* vf = v + lz;
+    const int sub = lane & 7, grp = lane >> 3;
+    for (int j = 0; j < kk; j++) {
+        const float* win = S.partial + ((size_t)pr.item * K + j) * S.win;
+        float sum = 0.f;
+        for (int f = sub; f - sub < lx; f += 8) {
+            if (f >= lx) continue;
+            const float wf = vf[f];
+            for (int row = grp; row < lz; row += 4) sum += win[row * lx + f] * (v[row] * wf);
+        }
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) S.receivers[(size_t)(S.n + j - 1) * S.rec.count + pr.item] = sum;
+    }
+}
+
+// Flags (word 0) a nonzero halo value in slots [0, nslots) of a 2D grid.
+__global__ void halo_nonzero(const float* __restrict__ u, Layout L, int nslots,
+                             int* __restrict__ flag) {
+    const int r = L.r;
+    const long long nz = L.nz, nx = L.nx;
+    const long long per = 2LL * r * nx + 2LL * r * (nz - 2 * r);  // halo points a slot
+    const long long total = per * nslots;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long s = i / per, k = i - s * per;
+        long long z, x;
+        if (k < 2LL * r * nx) {
+            const long long row = k / nx;
+            z = row < r ? row : nz - 2 * r + row;
+            x = k - row * nx;
+        } else {
+            const long long m = k - 2LL * r * nx, row = m / (2 * r), c = m - row * (2 * r);
+            z = r + row;
+            x = c < r ? c : nx - 2 * r + c;
+        }
+        if (u[s * L.slot + L.at2(z, x)] != 0.f) atomicOr(flag, 1);
+    }
+}
+
+__global__ void set_stops(Shot* shots, int nshots, int steps) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nshots) {
+        const long long stop = (long long)shots[s].n + steps - 1;
+        shots[s].stop = (int)(stop < shots[s].end ? stop : shots[s].end);
+    }
+}
+
 // One shot: grid (x tiles, z tiles).
 template <int R, bool VD, int TZ>
 __global__ void __launch_bounds__(kThreads)
@@ -291,7 +739,7 @@ __global__ void sources_batched(const Shot* __restrict__ shots,
 // axis 1 (x edges) or 0 (z edges) of every shot; one block per shot
 __global__ void edges_batched(const Shot* __restrict__ shots, int axis) {
     const Shot& S = shots[blockIdx.x];
-    if (!active(S)) return;
+    if (!active(S) || S.depth > 1) return;  // time-blocked shots apply their own
     const int before = S.bc[2 * axis], after = S.bc[2 * axis + 1];
     if (!before && !after) return;
     float* un;
@@ -321,7 +769,12 @@ __global__ void receivers_batched(const Shot* __restrict__ shots,
 
 __global__ void advance_batched(Shot* shots, int nshots) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < nshots && shots[s].n <= shots[s].end) shots[s].n++;
+    if (s < nshots && shots[s].n <= shots[s].stop) {
+        const int k = shots[s].depth;
+        const int left = shots[s].stop - shots[s].n + 1;
+        shots[s].n += k > 1 ? (k < left ? k : left) : 1;
+        if (k > 1) *shots[s].pairp ^= 1;  // the launch left its levels in the other pair
+    }
 }
 
 __global__ void swap_regions(float* __restrict__ a, float* __restrict__ b, long long n) {
@@ -354,10 +807,32 @@ struct HostShot {
     Shot d;                  // descriptor (host copy; n tracked on the host too)
     float* cq = nullptr;     // engine-owned C and Q
     int* slots = nullptr;    // engine-owned schedule
+    unsigned char* keep = nullptr;  // engine-owned per-step last-write flags
+    float* partial = nullptr;       // engine-owned receiver partials (time-blocked)
+    size_t partial_cap = 0;
     std::vector<int> perm;   // final logical -> physical slots
+    std::vector<int> table;  // per step: prev, cur, next physical slots
+    std::vector<size_t> rec_iv;  // receiver windows (host copy)
+    float* ext = nullptr;    // engine-owned level pairs (time-blocked)
+    int* pairp = nullptr;
+    bool in_pairs = false;   // the latest levels live in `ext`, not the slots
     long long grid = 0;      // elements of one pitched grid
+    // time blocking needs: constant density, each step reading the levels
+    // the two steps before it wrote, source windows off the halo
+    bool blockable = false;
     bool finished_restored = false;
 };
+
+// Steps per launch for shot `h` when its radius asks for `k`: k where the
+// shot allows time blocking (and its interior is wide enough for the edge
+// rules to stay within one side), else 1.
+static int effective_depth(const HostShot& h, int k) {
+    const Layout& L = h.d.L;
+    const int r = L.r;
+    if (k <= 1 || !h.blockable || !tb_supported(r, k)) return 1;
+    if (L.nz - 2 * r < 4 * r + 2 || L.nx - 2 * r < 4 * r + 2) return 1;
+    return k;
+}
 
 template <int R, bool VD, int TZ>
 static void set_smem_attr() {
@@ -388,6 +863,43 @@ static void launch_group_r(bool configure, int tz, const Shot* shots, const Tile
     if (tz == 8) launch_group_t<R, VD, 8>(configure, shots, tiles, ntiles, st);
     else if (tz == 32) launch_group_t<R, VD, 32>(configure, shots, tiles, ntiles, st);
     else launch_group_t<R, VD, 16>(configure, shots, tiles, ntiles, st);
+}
+
+template <int R, int K>
+static void launch_tblock_t(bool configure, const Shot* shots, const TileRef* tiles,
+                            const TbRec* trec, int ntiles, cudaStream_t st) {
+    if constexpr (tb_supported(R, K)) {
+        constexpr int HX = (R + 3) & ~3;
+        const int bytes = 2 * kTbRows * (128 + 2 * HX) * 4;
+        if (configure) {
+            cudaFuncSetAttribute(stencil2d_tblock<R, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 bytes);
+            return;
+        }
+        stencil2d_tblock<R, K><<<ntiles, kThreads, bytes, st>>>(shots, tiles, trec);
+    } else {
+        fail(SIMWAVE_E_ARGUMENT, "time-block depth too large for the space order");
+    }
+}
+
+template <int R>
+static void launch_tblock_r(bool configure, int k, const Shot* shots, const TileRef* tiles,
+                            const TbRec* trec, int ntiles, cudaStream_t st) {
+    if (k == 2) launch_tblock_t<R, 2>(configure, shots, tiles, trec, ntiles, st);
+    else if (k == 3) launch_tblock_t<R, 3>(configure, shots, tiles, trec, ntiles, st);
+    else launch_tblock_t<R, 4>(configure, shots, tiles, trec, ntiles, st);
+}
+
+static void launch_tblock(bool configure, int r, int k, const Shot* shots, const TileRef* tiles,
+                          const TbRec* trec, int ntiles, cudaStream_t st) {
+#define SB_T(RR)                                                                          \
+    case RR:                                                                              \
+        launch_tblock_r<RR>(configure, k, shots, tiles, trec, ntiles, st);                \
+        break;
+    switch (r) {
+        SB_T(1) SB_T(2) SB_T(3) SB_T(4) SB_T(5) SB_T(6) SB_T(7) SB_T(8) SB_T(9) SB_T(10)
+    }
+#undef SB_T
 }
 
 static void launch_group(bool configure, int r, bool vd, int tz, const Shot* shots,
@@ -428,6 +940,7 @@ struct Engine {
     std::vector<HostShot> shots;
     int next_id = 1;
     int tile_rows[kMaxRadius + 1];  // TZ per radius (tuning)
+    int depth[kMaxRadius + 1];      // steps per launch per radius (tuning; 1 = per step)
     // device tables (rebuilt when the shot set changes)
     Shot* d_shots = nullptr;
     size_t cap_shots = 0;
@@ -437,13 +950,19 @@ struct Engine {
     size_t cap_src = 0;
     PairRef* d_rec = nullptr;
     size_t cap_rec = 0;
+    TbRec* d_trec = nullptr;     // receiver-window parts of time-blocked tiles
+    size_t cap_trec = 0;
+    PairRef* d_tbrec = nullptr;  // receivers of time-blocked shots
+    size_t cap_tbrec = 0;
     struct Group {
         int r;
         bool vd;
+        int depth;
         int first, count;  // range in d_tiles
     };
     std::vector<Group> groups;
-    int nsrc_pairs = 0, nrec_pairs = 0;
+    int nsrc_pairs = 0, nrec_pairs = 0, ntb_rec = 0;
+    bool any_stepwise = false;
     bool dirty = true;
     // graph of `graph_steps` steps
     cudaGraphExec_t exec = nullptr;
@@ -451,7 +970,10 @@ struct Engine {
     size_t kernel_launches = 0;
 
     Engine() {
-        for (int r = 0; r <= kMaxRadius; r++) tile_rows[r] = 16;
+        for (int r = 0; r <= kMaxRadius; r++) {
+            tile_rows[r] = 16;
+            depth[r] = 1;
+        }
     }
 
     template <typename P>
@@ -470,38 +992,139 @@ struct Engine {
         graph_steps = 0;
     }
 
+    // Puts the shot's latest two levels where its next launches read them:
+    // into pair 0 of its level pairs (time-blocked) or back into the
+    // schedule's slots (per step). Runs between launches, on the engine
+    // stream.
+    void move_levels(HostShot& h, bool blocked) {
+        const size_t bytes = (size_t)h.grid * sizeof(float);
+        const bool running = h.d.n <= h.d.end;
+        const size_t i = (size_t)(h.d.n - h.d.begin);
+        if (blocked && !h.in_pairs) {
+            if (!h.ext) {
+                SB_CUDA(cudaMalloc(&h.ext, 4 * bytes));
+                SB_CUDA(cudaMalloc(&h.pairp, sizeof(int)));
+            }
+            SB_CUDA(cudaMemsetAsync(h.pairp, 0, sizeof(int), stream));
+            if (running) {
+                for (int l = 0; l < 2; l++)
+                    SB_CUDA(cudaMemcpyAsync(h.ext + l * h.grid,
+                                            h.d.u + (long long)h.table[3 * i + l] * h.d.L.slot,
+                                            bytes, cudaMemcpyDeviceToDevice, stream));
+            }
+            h.in_pairs = true;
+        } else if (!blocked && h.in_pairs) {
+            int pair = 0;
+            SB_CUDA(cudaMemcpyAsync(&pair, h.pairp, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            SB_CUDA(cudaStreamSynchronize(stream));
+            if (running) {
+                for (int l = 0; l < 2; l++)
+                    SB_CUDA(cudaMemcpyAsync(h.d.u + (long long)h.table[3 * i + l] * h.d.L.slot,
+                                            h.ext + (2 * pair + l) * h.grid, bytes,
+                                            cudaMemcpyDeviceToDevice, stream));
+            }
+            h.in_pairs = false;
+        }
+        h.d.ext = h.ext;
+        h.d.pairp = h.pairp;
+        h.d.grid = h.grid;
+    }
+
     // rebuild the device tables from the host shots (descriptors keep the
     // host-tracked step counters, which equal the device ones between runs)
     void rebuild() {
         const size_t ns = shots.size();
         grow(d_shots, cap_shots, ns);
         std::vector<Shot> desc(ns);
-        std::map<std::pair<int, int>, std::vector<TileRef>> byg;
-        std::vector<PairRef> srcp, recp;
+        std::map<std::tuple<int, int, int>, std::vector<TileRef>> byg;
+        std::vector<PairRef> srcp, recp, tbrecp;
+        std::vector<TbRec> trec;
+        any_stepwise = false;
         for (size_t i = 0; i < ns; i++) {
-            const HostShot& h = shots[i];
-            desc[i] = h.d;
+            HostShot& h = shots[i];
             const Layout& L = h.d.L;
             const int r = L.r;
-            const int tz = tile_rows[r];
-            const int nt_z = (int)((L.nz - 2 * r + tz - 1) / tz);
-            const int nt_x = (int)((L.nx - 2 * r + 127) / 128);
-            auto& v = byg[{r, h.d.den ? 1 : 0}];
-            for (int a = 0; a < nt_z; a++)
-                for (int b = 0; b < nt_x; b++) v.push_back({(int)i, a, b});
-            for (size_t s = 0; s < h.d.src.count; s++) srcp.push_back({(int)i, (int)s});
-            for (size_t s = 0; s < h.d.rec.count; s++) recp.push_back({(int)i, (int)s});
+            const int k = effective_depth(h, depth[r]);
+            h.d.depth = k;
+            move_levels(h, k > 1);
+            if (k > 1) {
+                int win = 1;
+                for (size_t q = 0; q < h.d.rec.count; q++) {
+                    const size_t* b = &h.rec_iv[4 * q];
+                    win = std::max(win, (int)((b[1] - b[0] + 1) * (b[3] - b[2] + 1)));
+                }
+                const size_t need = h.d.rec.count * (size_t)k * win;
+                if (need > h.partial_cap) {
+                    if (h.partial) cudaFree(h.partial);
+                    h.partial = nullptr;
+                    h.partial_cap = 0;
+                    SB_CUDA(cudaMalloc(&h.partial, std::max<size_t>(need, 4) * sizeof(float)));
+                    h.partial_cap = std::max<size_t>(need, 4);
+                }
+                h.d.partial = h.partial;
+                h.d.win = win;
+                const TbGeom g = tb_geom(r, k);
+                const int nt_z = tb_tiles(L.nz - 2 * r, g.oz);
+                const int nt_x = tb_tiles(L.nx - 2 * r, g.ox);
+                // each window point is copied by the tile that owns it
+                std::vector<std::vector<TbRec>> per(nt_z * nt_x);
+                for (size_t q = 0; q < h.d.rec.count; q++) {
+                    const size_t* b = &h.rec_iv[4 * q];
+                    const int z0 = tb_tile_of((long long)b[0], r, L.nz, g.oz);
+                    const int z1 = tb_tile_of((long long)b[1], r, L.nz, g.oz);
+                    const int x0 = tb_tile_of((long long)b[2], r, L.nx, g.ox);
+                    const int x1 = tb_tile_of((long long)b[3], r, L.nx, g.ox);
+                    for (int a = z0; a <= z1; a++)
+                        for (int c = x0; c <= x1; c++) {
+                            const int lo_z = a == 0 ? 0 : r + a * g.oz;
+                            const int hi_z = a == nt_z - 1 ? (int)L.nz : r + (a + 1) * g.oz;
+                            const int lo_x = c == 0 ? 0 : r + c * g.ox;
+                            const int hi_x = c == nt_x - 1 ? (int)L.nx : r + (c + 1) * g.ox;
+                            TbRec e;
+                            e.rc = (int)q;
+                            e.z0 = std::max(lo_z, (int)b[0]);
+                            e.z1 = std::min(hi_z, (int)b[1] + 1);
+                            e.x0 = std::max(lo_x, (int)b[2]);
+                            e.x1 = std::min(hi_x, (int)b[3] + 1);
+                            e.b0 = (int)b[0];
+                            e.b2 = (int)b[2];
+                            e.lx = (int)(b[3] - b[2] + 1);
+                            if (e.z1 > e.z0 && e.x1 > e.x0) per[a * nt_x + c].push_back(e);
+                        }
+                    tbrecp.push_back({(int)i, (int)q});
+                }
+                auto& v = byg[{r, 0, k}];
+                for (int a = 0; a < nt_z; a++)
+                    for (int c = 0; c < nt_x; c++) {
+                        const auto& e = per[a * nt_x + c];
+                        v.push_back({(int)i, a, c, (int)trec.size(), (int)e.size()});
+                        trec.insert(trec.end(), e.begin(), e.end());
+                    }
+            } else {
+                any_stepwise = true;
+                const int tz = tile_rows[r];
+                const int nt_z = (int)((L.nz - 2 * r + tz - 1) / tz);
+                const int nt_x = (int)((L.nx - 2 * r + 127) / 128);
+                auto& v = byg[{r, h.d.den ? 1 : 0, 1}];
+                for (int a = 0; a < nt_z; a++)
+                    for (int b = 0; b < nt_x; b++) v.push_back({(int)i, a, b, 0, 0});
+                for (size_t q = 0; q < h.d.src.count; q++) srcp.push_back({(int)i, (int)q});
+                for (size_t q = 0; q < h.d.rec.count; q++) recp.push_back({(int)i, (int)q});
+            }
+            desc[i] = h.d;
         }
         std::vector<TileRef> all;
         groups.clear();
         for (auto& kv : byg) {
-            groups.push_back({kv.first.first, kv.first.second != 0, (int)all.size(),
-                              (int)kv.second.size()});
+            groups.push_back({std::get<0>(kv.first), std::get<1>(kv.first) != 0,
+                              std::get<2>(kv.first), (int)all.size(), (int)kv.second.size()});
             all.insert(all.end(), kv.second.begin(), kv.second.end());
         }
         grow(d_tiles, cap_tiles, all.size());
         grow(d_src, cap_src, srcp.size());
         grow(d_rec, cap_rec, recp.size());
+        grow(d_trec, cap_trec, trec.size());
+        grow(d_tbrec, cap_tbrec, tbrecp.size());
         if (ns) SB_CUDA(cudaMemcpyAsync(d_shots, desc.data(), ns * sizeof(Shot),
                                         cudaMemcpyHostToDevice, stream));
         if (!all.empty())
@@ -513,43 +1136,73 @@ struct Engine {
         if (!recp.empty())
             SB_CUDA(cudaMemcpyAsync(d_rec, recp.data(), recp.size() * sizeof(PairRef),
                                     cudaMemcpyHostToDevice, stream));
+        if (!trec.empty())
+            SB_CUDA(cudaMemcpyAsync(d_trec, trec.data(), trec.size() * sizeof(TbRec),
+                                    cudaMemcpyHostToDevice, stream));
+        if (!tbrecp.empty())
+            SB_CUDA(cudaMemcpyAsync(d_tbrec, tbrecp.data(), tbrecp.size() * sizeof(PairRef),
+                                    cudaMemcpyHostToDevice, stream));
         SB_CUDA(cudaStreamSynchronize(stream));
         nsrc_pairs = (int)srcp.size();
         nrec_pairs = (int)recp.size();
-        for (const Group& g : groups)
-            launch_group(true, g.r, g.vd, tile_rows[g.r], nullptr, nullptr, 0, stream);
+        ntb_rec = (int)tbrecp.size();
+        for (const Group& g : groups) {
+            if (g.depth > 1)
+                launch_tblock(true, g.r, g.depth, nullptr, nullptr, nullptr, 0, stream);
+            else
+                launch_group(true, g.r, g.vd, tile_rows[g.r], nullptr, nullptr, 0, stream);
+        }
         drop_graph();
         dirty = false;
     }
 
-    // one step of every shot
+    // kernels of one step (one block of steps for the time-blocked shots)
+    size_t step_launches() const {
+        return groups.size() + (nsrc_pairs ? 1 : 0) + (any_stepwise ? 2 : 0) +
+               (nrec_pairs ? 1 : 0) + (ntb_rec ? 1 : 0) + 1;
+    }
+
+    // one step of every per-step shot, one block of steps of every
+    // time-blocked shot
     void enqueue_step(cudaStream_t st) {
         for (const Group& g : groups) {
-            launch_group(false, g.r, g.vd, tile_rows[g.r], d_shots, d_tiles + g.first, g.count,
-                         st);
+            if (g.depth > 1)
+                launch_tblock(false, g.r, g.depth, d_shots, d_tiles + g.first, d_trec, g.count,
+                              st);
+            else
+                launch_group(false, g.r, g.vd, tile_rows[g.r], d_shots, d_tiles + g.first,
+                             g.count, st);
             SB_CUDA(cudaGetLastError());
         }
         if (nsrc_pairs) sources_batched<<<nsrc_pairs, 128, 0, st>>>(d_shots, d_src);
         const int ns = (int)shots.size();
-        edges_batched<<<ns, 256, 0, st>>>(d_shots, 1);
-        edges_batched<<<ns, 256, 0, st>>>(d_shots, 0);
+        if (any_stepwise) {
+            edges_batched<<<ns, 256, 0, st>>>(d_shots, 1);
+            edges_batched<<<ns, 256, 0, st>>>(d_shots, 0);
+        }
         if (nrec_pairs)
             receivers_batched<<<(nrec_pairs * 32 + 255) / 256, 256, 0, st>>>(d_shots, d_rec,
                                                                              nrec_pairs);
+        if (ntb_rec)
+            receivers_tblock<<<(ntb_rec * 32 + 255) / 256, 256, 0, st>>>(d_shots, d_tbrec,
+                                                                          ntb_rec);
         advance_batched<<<(ns + 127) / 128, 128, 0, st>>>(d_shots, ns);
         SB_CUDA(cudaGetLastError());
     }
 
+    // Advances every shot by `steps` time steps (or to its end).
     void run(int steps, cudaStream_t user) {
         if (dirty) rebuild();
         if (shots.empty() || steps <= 0) return;
-        // the longest remaining shot bounds the useful steps
-        int most = 0;
-        for (const HostShot& h : shots) most = std::max(most, h.d.end - h.d.n + 1);
-        steps = std::min(steps, most);
-        if (steps <= 0) return;
+        // launches needed: the most blocks any shot needs for its steps
+        int blocks = 0;
+        for (const HostShot& h : shots) {
+            const int left = std::min(steps, h.d.end - h.d.n + 1);
+            if (left > 0) blocks = std::max(blocks, (left + h.d.depth - 1) / h.d.depth);
+        }
+        if (blocks <= 0) return;
         const int K = 16;  // steps per graph
-        if (!exec && steps >= K) {
+        if (!exec && blocks >= K) {
             cudaGraph_t graph;
             SB_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             try {
@@ -568,14 +1221,19 @@ struct Engine {
         SB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         SB_CUDA(cudaEventRecord(ev, user));
         SB_CUDA(cudaStreamWaitEvent(stream, ev, 0));
+        // each shot stops after `steps` more steps, however many launches run
+        const int ns = (int)shots.size();
+        set_stops<<<(ns + 127) / 128, 128, 0, stream>>>(d_shots, ns, steps);
+        SB_CUDA(cudaGetLastError());
+        kernel_launches += 1;
         int done = 0;
-        const size_t per_step = groups.size() + (nsrc_pairs ? 1 : 0) + 3 + (nrec_pairs ? 1 : 0);
-        while (steps - done >= K && exec) {
+        const size_t per_step = step_launches();
+        while (blocks - done >= K && exec) {
             SB_CUDA(cudaGraphLaunch(exec, stream));
             done += K;
             kernel_launches += K * per_step;
         }
-        for (; done < steps; done++) {
+        for (; done < blocks; done++) {
             enqueue_step(stream);
             kernel_launches += per_step;
         }
@@ -665,6 +1323,7 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
         }
     }
     h.perm = perm;
+    h.table = table;
     h.grid = grid;
     Shot& d = h.d;
     std::memset(&d, 0, sizeof(d));
@@ -697,11 +1356,69 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
     d.end = (int)P->end_timestep;
     d.n = d.begin;
     for (int e = 0; e < 4; e++) d.bc[e] = (int)P->boundary_conditions[e];
+    d.stop = d.end;
+    d.depth = 1;
+    // last-write flags (a level of a time block goes back to its slot when no
+    // later step overwrites that slot) and the level chain time blocking
+    // relies on: each step reads the levels the two steps before it wrote
+    const size_t nsteps = table.size() / 3;
+    std::vector<unsigned char> keep(nsteps, 0);
+    {
+        std::vector<char> seen(nsl + 1, 0);
+        for (size_t i = nsteps; i-- > 0;) {
+            const int slot = table[3 * i + 2];
+            if (!seen[slot]) keep[i] = 1;
+            seen[slot] = 1;
+        }
+    }
+    bool chain = true;
+    for (size_t i = 1; i < nsteps; i++)
+        chain = chain && table[3 * i] == table[3 * (i - 1) + 1] &&
+                table[3 * i + 1] == table[3 * (i - 1) + 2];
+    // window tables to the host: receivers for the tile lists, sources for
+    // the halo test
+    h.rec_iv.assign(4 * P->num_receivers, 0);
+    std::vector<size_t> src_iv(4 * P->num_sources, 0);
+    if (P->num_receivers)
+        SB_CUDA(cudaMemcpyAsync(h.rec_iv.data(), P->rec_points_interval,
+                                h.rec_iv.size() * sizeof(size_t), cudaMemcpyDeviceToHost,
+                                E.stream));
+    if (P->num_sources)
+        SB_CUDA(cudaMemcpyAsync(src_iv.data(), P->src_points_interval,
+                                src_iv.size() * sizeof(size_t), cudaMemcpyDeviceToHost,
+                                E.stream));
+    SB_CUDA(cudaStreamSynchronize(E.stream));
+    bool src_inside = true;
+    for (size_t q = 0; q < P->num_sources; q++) {
+        const size_t* b = &src_iv[4 * q];
+        src_inside = src_inside && b[0] >= (size_t)r && b[1] < P->nz - r && b[2] >= (size_t)r &&
+                     b[3] < P->nx - r;
+    }
+    h.blockable = !vd && chain && src_inside;
+    {
+        int* flag = nullptr;
+        SB_CUDA(cudaMalloc(&flag, sizeof(int)));
+        SB_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), E.stream));
+        halo_nonzero<<<256, 256, 0, E.stream>>>(d.u, d.L, (int)nsl, flag);
+        int nonzero = 1;
+        const cudaError_t launched = cudaGetLastError();
+        const cudaError_t copied =
+            cudaMemcpyAsync(&nonzero, flag, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+        const cudaError_t synced = cudaStreamSynchronize(E.stream);
+        cudaFree(flag);
+        SB_CUDA(launched);
+        SB_CUDA(copied);
+        SB_CUDA(synced);
+        d.halo_zero = nonzero == 0;
+    }
     // engine-owned: coefficients and schedule
     SB_CUDA(cudaMalloc(&h.cq, 2 * (size_t)grid * sizeof(float)));
     SB_CUDA(cudaMalloc(&h.slots, table.size() * sizeof(int)));
     SB_CUDA(cudaMemcpyAsync(h.slots, table.data(), table.size() * sizeof(int),
                             cudaMemcpyHostToDevice, E.stream));
+    SB_CUDA(cudaMalloc(&h.keep, std::max<size_t>(nsteps, 1)));
+    SB_CUDA(cudaMemcpyAsync(h.keep, keep.data(), nsteps, cudaMemcpyHostToDevice, E.stream));
+    d.keep = h.keep;
     form_coefficients(d.vel, d.damp, h.cq, h.cq + grid, grid, d.dt, E.stream);
     SB_CUDA(cudaGetLastError());
     // box where Q is zero (its loads are skipped there)
@@ -728,6 +1445,7 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
 
 static void release(Engine& E, size_t i, bool restore) {
     HostShot& h = E.shots[i];
+    E.move_levels(h, false);  // an unfinished time-blocked shot's levels go back to its slots
     if (restore) {
         // logical slot j ends in slot j, as in the reference
         const int nsl = (int)h.perm.size();
@@ -752,6 +1470,10 @@ static void release(Engine& E, size_t i, bool restore) {
     SB_CUDA(cudaStreamSynchronize(E.stream));
     cudaFree(h.cq);
     cudaFree(h.slots);
+    cudaFree(h.keep);
+    if (h.partial) cudaFree(h.partial);
+    if (h.ext) cudaFree(h.ext);
+    if (h.pairp) cudaFree(h.pairp);
     E.shots.erase(E.shots.begin() + (long)i);
     E.dirty = true;
 }
@@ -797,8 +1519,12 @@ struct Persist2D : Shot2D {
 // edges of its columns if it is a z-edge tile. Exact when the first and last
 // tiles hold at least r + 1 rows and columns (Shot2D::fused): every boundary
 // operation then reads and writes points of one tile only, in the
-// reference's order.
-__device__ void tile_sources_edges(const Shot2D& P, float* un, long long n, int tz, int tx) {
+// reference's order. With `ring`, the tile also saves its points of the
+// four interior edge lines between the sources and the boundary conditions
+// (rows r and nz - r - 1, then columns r and nx - r - 1 without the corner
+// rows: the layout of the adjoint's boundary ring).
+__device__ void tile_sources_edges(const Shot2D& P, float* un, long long n, int tz, int tx,
+                                   float* ring = nullptr) {
     const Layout& L = P.L;
     const int r = L.r;
     const int nz = (int)L.nz, nx = (int)L.nx;
@@ -828,6 +1554,23 @@ __device__ void tile_sources_edges(const Shot2D& P, float* un, long long n, int 
         }
     }
     __syncthreads();
+    if (ring) {
+        const int w = nx - 2 * r, h = nz - 2 * r - 2;
+        const int c0 = max(x_lo, r), c1 = min(x_hi, nx - r);
+        if (tz == 0)
+            for (int j = c0 + threadIdx.x; j < c1; j += blockDim.x) ring[j - r] = un[L.at2(r, j)];
+        if (tz == P.tiles_z - 1)
+            for (int j = c0 + threadIdx.x; j < c1; j += blockDim.x)
+                ring[w + j - r] = un[L.at2(nz - r - 1, j)];
+        const int i0 = max(z_lo, r + 1), i1 = min(z_hi, nz - r - 1);
+        if (tx == 0)
+            for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+                ring[2 * w + i - r - 1] = un[L.at2(i, r)];
+        if (tx == P.tiles_x - 1)
+            for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+                ring[2 * w + h + i - r - 1] = un[L.at2(i, nx - r - 1)];
+        __syncthreads();
+    }
     // x edges (rows of this tile), then z edges (columns of this tile)
     const int bx0 = P.bc[2], bx1 = P.bc[3], bz0 = P.bc[0], bz1 = P.bc[1];
     if ((bx0 && tx == 0) || (bx1 && tx == P.tiles_x - 1)) {
@@ -940,15 +1683,18 @@ stencil2d_persistent(const Persist2D P) {
 // One time step of a 2D shot in one launch: blocks [0, ntiles) compute a
 // tile each (stencil, then the sources and boundary edges the tile owns),
 // the blocks after them gather the receivers (they read u_cur only).
+// `ring` (optional) receives the interior edge lines before the boundary
+// conditions.
 template <int R, bool VD, int TZ>
 __global__ void __launch_bounds__(kThreads)
-stencil2d_step(const Shot2D P, float* un, const float* uc, const float* up, long long n) {
+stencil2d_step(const Shot2D P, float* un, const float* uc, const float* up, long long n,
+               float* ring) {
     if ((int)blockIdx.x < P.ntiles) {
         const int t = blockIdx.x;
         stencil2d_tile<R, VD, TZ>(reinterpret_cast<float*>(sw_batch_smem), P.L, un, uc, up, P.C,
                                   P.Q, P.den, P.W, P.zb, t / P.tiles_x, t % P.tiles_x);
         __syncthreads();
-        tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x);
+        tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x, ring);
         return;
     }
     const long long w = ((long long)(blockIdx.x - P.ntiles) * blockDim.x + threadIdx.x) >> 5;
@@ -960,7 +1706,7 @@ stencil2d_step(const Shot2D P, float* un, const float* uc, const float* up, long
 
 template <int R, bool VD>
 static void step_r(const Shot2D& P, float* un, const float* uc, const float* up, long long n,
-                   cudaStream_t st) {
+                   float* ring, cudaStream_t st) {
     constexpr int TZ = 16;
     constexpr int HX = (R + 3) & ~3;
     const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
@@ -973,7 +1719,8 @@ static void step_r(const Shot2D& P, float* un, const float* uc, const float* up,
         configured[dev & 63] = true;
     }
     const int rec_blocks = (int)((P.rec.count + kWarps - 1) / kWarps);
-    stencil2d_step<R, VD, TZ><<<P.ntiles + rec_blocks, kThreads, bytes, st>>>(P, un, uc, up, n);
+    stencil2d_step<R, VD, TZ><<<P.ntiles + rec_blocks, kThreads, bytes, st>>>(P, un, uc, up, n,
+                                                                               ring);
 }
 
 template <int R, bool VD>
@@ -1042,11 +1789,11 @@ bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
 }
 
 void step2d_launch(const Shot2D& S, bool vd, float* un, const float* uc, const float* up,
-                   long long n, cudaStream_t st) {
+                   long long n, cudaStream_t st, float* ring) {
 #define SB_ST(RR)                                                               \
     case RR:                                                                    \
-        if (vd) batch::step_r<RR, true>(S, un, uc, up, n, st);                  \
-        else batch::step_r<RR, false>(S, un, uc, up, n, st);                    \
+        if (vd) batch::step_r<RR, true>(S, un, uc, up, n, ring, st);            \
+        else batch::step_r<RR, false>(S, un, uc, up, n, ring, st);              \
         break;
     switch (S.L.r) {
         SB_ST(1) SB_ST(2) SB_ST(3) SB_ST(4) SB_ST(5) SB_ST(6) SB_ST(7) SB_ST(8) SB_ST(9) SB_ST(10)
@@ -1119,6 +1866,8 @@ extern "C" int simwave_batch_destroy(simwave_batch* b) {
         cudaFree(e->d_tiles);
         cudaFree(e->d_src);
         cudaFree(e->d_rec);
+        cudaFree(e->d_trec);
+        cudaFree(e->d_tbrec);
         cudaStreamDestroy(e->stream);
         delete e;
     });
@@ -1177,6 +1926,35 @@ extern "C" int simwave_batch_set_tile_rows(simwave_batch* b, int space_order, in
         Engine* e = sw::batch::engine(b);
         e->tile_rows[space_order / 2] = rows;
         e->dirty = true;
+    });
+}
+
+extern "C" int simwave_batch_set_depth(simwave_batch* b, int space_order, int depth) {
+    return sw::batch::guarded([&] {
+        if (!b || space_order < 2 || space_order > 20 || space_order % 2 || depth < 1 ||
+            depth > 4 || (depth > 1 && !sw::batch::tb_supported(space_order / 2, depth)))
+            sw::batch::fail(SIMWAVE_E_ARGUMENT,
+                            "space_order even in 2..20; depth 1, or 2..4 with (depth x "
+                            "space_order / 2) <= 32 and the tile's owned width >= 64");
+        std::lock_guard<std::mutex> lock(sw::batch::g_mutex);
+        Engine* e = sw::batch::engine(b);
+        e->depth[space_order / 2] = depth;
+        e->dirty = true;
+    });
+}
+
+extern "C" int simwave_batch_depth(simwave_batch* b, int shot_id, int* depth) {
+    return sw::batch::guarded([&] {
+        if (!b || !depth) sw::batch::fail(SIMWAVE_E_ARGUMENT, "null argument");
+        std::lock_guard<std::mutex> lock(sw::batch::g_mutex);
+        Engine* e = sw::batch::engine(b);
+        if (e->dirty) e->rebuild();
+        for (const auto& h : e->shots)
+            if (h.id == shot_id) {
+                *depth = h.d.depth;
+                return;
+            }
+        sw::batch::fail(SIMWAVE_E_ARGUMENT, "unknown shot id");
     });
 }
 

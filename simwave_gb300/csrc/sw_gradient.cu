@@ -353,9 +353,6 @@ static void prepare_coefficients(Ctx& X, Scratch& mem, bool aligned) {
     GR_CUDA(cudaStreamSynchronize(mem.st));
     const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
     for (int i = 0; i < 6; i++) X.zero_box[i] = good ? box[i] : 0;
-    // Dirichlet runs save the boundary lines between the sources and the
-    // boundary conditions of each step: those keep separate launches
-    if (X.dirichlet) return;
     X.fused = shot2d_prepare(X.shot, X.L, X.C, X.Q, nullptr, X.vel, X.damp, X.W, X.zero_box,
                              X.src, X.wavelet, X.wavelet_count, X.dt, X.rec, X.receivers,
                              X.bc) &&
@@ -387,9 +384,10 @@ static void stencil(const Ctx& X, float* un, const float* uc, const float* up,
 // `ring_row`, the record of u^n into `rec_row` (either may be null).
 static void forward_step(const Ctx& X, float* un, const float* uc, const float* up,
                          size_t n, float* ring_row, float* rec_row, cudaStream_t st) {
-    if (X.fused && !ring_row) {
+    if (X.fused) {
         // the record goes to X.receivers + (n - 1) * count, where rec_row points
-        step2d_launch(rec_row ? X.shot : X.shot_quiet, false, un, uc, up, (long long)n, st);
+        step2d_launch(rec_row ? X.shot : X.shot_quiet, false, un, uc, up, (long long)n, st,
+                      ring_row);
         GR_LAUNCHED("stencil2d_step");
         return;
     }

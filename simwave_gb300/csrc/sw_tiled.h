@@ -81,9 +81,12 @@ bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
                     const Windows<float>& rec, float* receivers, const int* bc);
 
 // Step n of `S` (fused only) in one launch: stencil, sources, edges and the
-// record of u_cur.
+// record of u_cur. `ring` (optional, 2 (nx - 2r) + 2 (nz - 2r - 2) floats)
+// receives the interior edge lines after the sources, before the boundary
+// conditions: rows r and nz - r - 1, then columns r and nx - r - 1 without
+// the corner rows.
 void step2d_launch(const Shot2D& S, bool vd, float* un, const float* uc, const float* up,
-                   long long n, cudaStream_t st);
+                   long long n, cudaStream_t st, float* ring = nullptr);
 
 // Every step of `S` in one cooperative launch (small grids, where per-step
 // kernels are bound by their start-up): `slots` (device) holds the physical

@@ -75,7 +75,7 @@ class ShotServer:
     """Serve requests with continuous batching on one GPU."""
 
     def __init__(self, hbm_budget=None, epoch_steps=64, inflight=2, device="cuda",
-                 tile_rows=None, reserve_bytes=0, stage_workers=2):
+                 tile_rows=None, reserve_bytes=0, stage_workers=2, tuning=None):
         self.device = torch.device(device)
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
@@ -85,6 +85,8 @@ class ShotServer:
         self.engine = BatchEngine(device)
         for order, rows in (tile_rows or {}).items():
             self.engine.set_tile_rows(order, rows)
+        if tuning:  # {order: {"rows": r, "depth": k}} from batch.autotune
+            self.engine.apply(tuning)
         lo, hi = torch.cuda.Stream.priority_range()
         self.epoch_stream = torch.cuda.Stream(self.device, priority=hi)
         self.shot_stream = torch.cuda.Stream(self.device, priority=lo)
@@ -156,7 +158,7 @@ class ShotServer:
             req._staged = None
             if req.batchable:
                 self.epoch_stream.wait_event(uploaded)
-                sid = self.engine.add(req.problem)
+                sid = self.engine.add(req.problem, ready=uploaded)
                 self.active2d[sid] = req
             else:
                 req._uploaded = uploaded
