@@ -189,6 +189,25 @@ def batched_leg(nshots=96, max_side=2048):
     e1.record(stream)
     e1.synchronize()
     plain_s = e0.elapsed_time(e1) / 1e3
+    # drop-in: the reference-facing host call (what Solver.forward makes),
+    # one shot after another with host arrays in and out; one shot per order
+    # first so that no kernel is loaded inside the timing
+    import contextlib
+    import io
+    from simwave_gb300.backend.middleware import Middleware
+    mw = Middleware()
+
+    def dropin(k):
+        with contextlib.redirect_stdout(io.StringIO()):
+            mw.exec("forward", **dict(k, u_full=np.zeros_like(k["u_full"]),
+                                      shot_record=np.zeros_like(k["shot_record"])))
+
+    for order in sorted({int(k["space_order"]) for k in kws}):
+        dropin(next(k for k in kws if int(k["space_order"]) == order))
+    t0 = time.perf_counter()
+    for k in kws:
+        dropin(k)
+    dropin_s = time.perf_counter() - t0
     # batch: tile height and time-blocking depth picked per order, then one
     # engine for all shots
     tiles = autotune(probs)
@@ -209,10 +228,13 @@ def batched_leg(nshots=96, max_side=2048):
             "shots_per_s": round(nshots / batch_s, 2),
             "plain_shots_per_s": round(nshots / plain_s, 2),
             "speedup_vs_plain": round(plain_s / batch_s, 2),
+            "dropin_shots_per_s": round(nshots / dropin_s, 2),
+            "speedup_vs_dropin": round(dropin_s / batch_s, 2),
             "batch_gpts": round(updates / batch_s / 1e9, 2),
             "plain_gpts": round(updates / plain_s / 1e9, 2),
             "tuning": {str(k): v for k, v in tiles.items()}, "batch_launches": int(launches),
-            "timing": "CUDA events, resident inputs, setup excluded"}
+            "timing": "batch and plain: CUDA events, resident inputs, setup excluded; "
+                      "drop-in: wall clock of the host calls, copies included"}
 
 
 def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320,

@@ -320,6 +320,20 @@ stencil2d_batched(const Shot* __restrict__ shots, const TileRef* __restrict__ ti
 }
 
 // ---- time-blocked 2D stencil (constant density) -----------------------------------
+constexpr int kTbThreads = 512;
+constexpr int kTbWarps = kTbThreads / 32;
+
+// 16-byte asynchronous copy global -> shared (zero-filled when !ok).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src),
+                 "r"(ok ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Copies the owned points [zlo, zhi) x [xlo, xhi) of a staged buffer (row
 // pitch tw, region origin zr0, xc0) to the same points of grid g.
 __device__ __forceinline__ void tb_copy_owned(const float* buf, float* g, int tw, int zr0,
@@ -327,7 +341,7 @@ __device__ __forceinline__ void tb_copy_owned(const float* buf, float* g, int tw
                                               int pitch, int lead, int warp, int lane) {
     const int xa = xlo - ((lead + xlo) & 3);  // 16-byte aligned start
     const int nch = (xhi - xa + 3) / 4;
-    for (int zz = zlo + warp; zz < zhi; zz += kWarps) {
+    for (int zz = zlo + warp; zz < zhi; zz += kTbWarps) {
         const float* srow = buf + (zz - zr0) * tw - xc0;
         float* grow = g + (long long)zz * pitch + lead;
         for (int c = lane; c < nch; c += 32) {
@@ -354,12 +368,13 @@ __device__ __forceinline__ void tb_copy_owned(const float* buf, float* g, int tw
 // its slot only when it is one of the last two of the block (the next block
 // starts from them) or the last write to its slot (snapshots, final slots).
 template <int R, int K>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kTbThreads, 1)
 stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ tiles,
                  const TbRec* __restrict__ trec) {
     constexpr int HX = (R + 3) & ~3;
     constexpr int TW = 128 + 2 * HX;
     constexpr int TH = kTbRows;
+    constexpr int CR = TH - 2 * R;  // rows with computed points (C and Q staged)
     constexpr int NC = (4 + 2 * HX) / 4;
     constexpr TbGeom G = tb_geom(R, K);
     constexpr int MZ = G.mz, OZ = G.oz, DX = G.dx, OX = G.ox;
@@ -381,26 +396,35 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
     const int xhi = t.tx == tiles_x - 1 ? nx : R + (t.tx + 1) * OX;
     float* U = reinterpret_cast<float*>(sw_batch_smem);
     float* P = U + TH * TW;
+    float* Cs = P + TH * TW;  // [CR][128]: C of region rows R .. TH - R - 1
+    float* Qs = Cs + CR * 128;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int pair = *S.pairp;
     {
+        // u_prev, u_cur (region), C and Q (computed rows and columns), all
+        // in flight at once; points off the grid read as zero
         const float* up = S.ext + (long long)(2 * pair) * S.grid;
         const float* uc = up + S.grid;
         constexpr int CH = TW / 4;
-#pragma unroll 4
-        for (int i = threadIdx.x; i < TH * CH; i += kThreads) {
+        for (int i = threadIdx.x; i < TH * CH; i += kTbThreads) {
             const int row = i / CH, ch = i - row * CH;
             const int z = zr0 + row;
             const int col = lead + xc0 + 4 * ch;
-            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-            if (z >= 0 && z < nz && col >= 0 && col + 3 < pitch) {
-                const long long p = (long long)z * pitch + col;
-                a = *reinterpret_cast<const float4*>(uc + p);
-                b = *reinterpret_cast<const float4*>(up + p);
-            }
-            *reinterpret_cast<float4*>(U + row * TW + 4 * ch) = a;
-            *reinterpret_cast<float4*>(P + row * TW + 4 * ch) = b;
+            const bool ok = z >= 0 && z < nz && col >= 0 && col + 3 < pitch;
+            const long long p = ok ? (long long)z * pitch + col : 0;
+            cp_async16(U + row * TW + 4 * ch, uc + p, ok);
+            cp_async16(P + row * TW + 4 * ch, up + p, ok);
         }
+        for (int i = threadIdx.x; i < CR * 32; i += kTbThreads) {
+            const int row = i >> 5, ch = i & 31;
+            const int z = zr0 + R + row;
+            const int col = lead + xr0 + 4 * ch;
+            const bool ok = z >= R && z < nz - R && col >= 0 && col + 3 < pitch;
+            const long long p = ok ? (long long)z * pitch + col : 0;
+            cp_async16(Cs + row * 128 + 4 * ch, S.C + p, ok);
+            cp_async16(Qs + row * 128 + 4 * ch, S.Q + p, ok);
+        }
+        cp_async_wait_all();
     }
     P2 w2[R + 1];
 #pragma unroll
@@ -422,7 +446,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
     for (int j = 0; j < kk; j++) {
         const int n = n0 + j;
         // receivers: this tile's part of each window of level n, to scratch
-        for (int e = warp; e < t.rec_count; e += kWarps) {
+        for (int e = warp; e < t.rec_count; e += kTbWarps) {
             const TbRec q = trec[t.rec_first + e];
             const int w = q.x1 - q.x0;
             const int cnt = (q.z1 - q.z0) * w;
@@ -432,27 +456,14 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
                 dst[(z - q.b0) * q.lx + (xx - q.b2)] = U[(z - zr0) * TW + (xx - xc0)];
             }
         }
-        // stencil over the rows that stay exact after this step; each warp
-        // requests its next row's coefficients before computing this one
+        // stencil over the rows that stay exact after this step
         const int rlo = (j + 1) * R, rhi = TH - (j + 1) * R;
-        int rr = rlo + warp;
-        V4 cc_n = {{0ull}, {0ull}}, qq_n = {{0ull}, {0ull}};
-        bool qz_n = true;
-        auto fetch = [&](int row) {
-            const int z = zr0 + row;
-            const bool ok = row < rhi && z >= R && z < nz - R && xany;
-            const long long p = (long long)z * pitch + lead + x;
-            qz_n = xbox && z >= S.zb[0] && z < S.zb[1];
-            cc_n = ldg_v4(S.C + p, ok);
-            qq_n = ldg_v4(S.Q + p, ok && !qz_n);
-        };
-        fetch(rr);
-        for (; rr < rhi; rr += kWarps) {
-            const V4 cc = cc_n, qq = qq_n;
-            const bool qzero = qz_n;
-            fetch(rr + kWarps);
+        for (int rr = rlo + warp; rr < rhi; rr += kTbWarps) {
             const int z = zr0 + rr;
             if (z < R || z >= nz - R || !xany) continue;
+            const bool qzero = xbox && z >= S.zb[0] && z < S.zb[1];
+            const V4 cc = lds_v4(Cs + (rr - R) * 128 + 4 * lane);
+            const V4 qq = lds_v4(Qs + (rr - R) * 128 + 4 * lane);
             const float* tu = U + rr * TW + 4 * lane;
             const V4 u0 = lds_v4(tu + HX);
             V4 sz = vmul(w2[0], u0);
@@ -517,7 +528,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
             const int nr = max(0, cb - right0), per = nl + nr;
             const int A = (top + bot) * w, B = nm * per;
 #pragma unroll 4
-            for (int i = threadIdx.x; i < A + B; i += kThreads) {
+            for (int i = threadIdx.x; i < A + B; i += kTbThreads) {
                 int zz, xx;
                 if (i < A) {
                     const int row = i / w;
@@ -544,7 +555,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
                     continue;
                 const float* v = S.src.values + S.src.offsets[s];
                 const long long total = window_size<2>(b);
-                for (long long q = threadIdx.x; q < total; q += kThreads) {
+                for (long long q = threadIdx.x; q < total; q += kTbThreads) {
                     long long iz, ix, iy;
                     window_point<2>(b, q, iz, ix, iy);
                     const int z = (int)(b[0] + iz), xx = (int)(b[2] + ix);
@@ -564,7 +575,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
             const bool left = bx0 && R >= xc0 && R < xc0 + TW;
             const bool right = bx1 && nx - R - 1 >= xc0 && nx - R - 1 < xc0 + TW;
             if (left || right) {
-                for (int i = r0 + threadIdx.x; i < r1; i += kThreads) {
+                for (int i = r0 + threadIdx.x; i < r1; i += kTbThreads) {
                     float* row = P + (i - zr0) * TW - xc0;  // indexed by grid column
                     if (left) {
                         if (bx0 == 1) row[R] = 0.f;
@@ -586,7 +597,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
             const bool top = bz0 && R >= zr0 && R < zr0 + TH;
             const bool bottom = bz1 && nz - R - 1 >= zr0 && nz - R - 1 < zr0 + TH;
             if (top || bottom) {
-                for (int c = c0 + threadIdx.x; c < c1; c += kThreads) {
+                for (int c = c0 + threadIdx.x; c < c1; c += kTbThreads) {
                     float* col = P + (c - xc0) - zr0 * TW;  // indexed by grid row * TW
                     if (top) {
                         if (bz0 == 1) col[R * TW] = 0.f;
@@ -615,7 +626,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
         if (S.keep[n - S.begin]) {
             const int xa = xlo - ((lead + xlo) & 3);  // 16-byte aligned start
             const int nch = (xhi - xa + 3) / 4;
-            for (int zz = zlo + warp; zz < zhi; zz += kWarps) {
+            for (int zz = zlo + warp; zz < zhi; zz += kTbWarps) {
                 const bool zin = zz >= R && zz < nz - R;
                 const float* srow = P + (zz - zr0) * TW - xc0;
                 float* grow = un + (long long)zz * pitch + lead;
@@ -870,13 +881,13 @@ static void launch_tblock_t(bool configure, const Shot* shots, const TileRef* ti
                             const TbRec* trec, int ntiles, cudaStream_t st) {
     if constexpr (tb_supported(R, K)) {
         constexpr int HX = (R + 3) & ~3;
-        const int bytes = 2 * kTbRows * (128 + 2 * HX) * 4;
+        const int bytes = (2 * kTbRows * (128 + 2 * HX) + 2 * (kTbRows - 2 * R) * 128) * 4;
         if (configure) {
             cudaFuncSetAttribute(stencil2d_tblock<R, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  bytes);
             return;
         }
-        stencil2d_tblock<R, K><<<ntiles, kThreads, bytes, st>>>(shots, tiles, trec);
+        stencil2d_tblock<R, K><<<ntiles, kTbThreads, bytes, st>>>(shots, tiles, trec);
     } else {
         fail(SIMWAVE_E_ARGUMENT, "time-block depth too large for the space order");
     }
