@@ -233,8 +233,9 @@ def batched_leg(nshots=96, max_side=2048):
             "batch_gpts": round(updates / batch_s / 1e9, 2),
             "plain_gpts": round(updates / plain_s / 1e9, 2),
             "tuning": {str(k): v for k, v in tiles.items()}, "batch_launches": int(launches),
-            "timing": "batch and plain: CUDA events, resident inputs, setup excluded; "
-                      "drop-in: wall clock of the host calls, copies included"}
+            "timing": "CUDA events, inputs resident; batch: admission, steps and release "
+                      "of all shots; plain: one device call per shot (its own preparation "
+                      "included); drop-in: wall clock of the host calls, copies included"}
 
 
 def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320,

@@ -149,31 +149,53 @@ def _candidates(order, rows, depths, device):
     return out
 
 
-def autotune(problems, steps=64, rows=TILE_ROWS, depths=DEPTHS):
+def _time_engine(problems, tuning, steps):
+    """Seconds for ``steps`` steps of all ``problems`` in one engine set to
+    ``tuning`` (after ``steps`` untimed ones)."""
+    eng = BatchEngine(problems[0].device)
+    try:
+        eng.apply(tuning)
+        for p in problems:
+            p.reset()
+            eng.add(p)
+        eng.run(steps)  # warm-up (graph capture, kernel load)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.run(steps)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+    finally:
+        eng.close()
+
+
+def autotune(problems, steps=64, rows=TILE_ROWS, depths=DEPTHS, margin=0.03):
     """Pick the tile height and the time-blocking depth per space order by
-    timing ``steps`` steps of the given shots with every candidate; returns
-    ``{order: {"rows": r, "depth": k}}`` (``BatchEngine.apply`` takes it)."""
+    timing; returns ``{order: {"rows": r, "depth": k}}`` (``BatchEngine.apply``
+    takes it).
+
+    Tile heights are timed on each order's shots alone (only that order's
+    stencil launch changes). Depths are timed on all the shots together, one
+    order at a time: the per-step source, boundary and receiver launches are
+    shared by every order's per-step shots, so an order's shots timed alone
+    would charge them all to that order. A depth is kept only when the whole
+    set runs at least ``margin`` faster with it.
+    """
     orders = sorted({int(p.problem.space_order) for p in problems})
     best = {}
     for order in orders:
         group = [p for p in problems if int(p.problem.space_order) == order]
-        timings = {}
-        for r, k in _candidates(order, rows, depths, group[0].device):
-            eng = BatchEngine(group[0].device)
-            eng.set_tile_rows(order, r)
-            eng.set_depth(order, k)
-            for p in group:
-                p.reset()
-                eng.add(p)
-            eng.run(steps)  # warm-up (graph capture, kernel load)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            eng.run(steps)
-            torch.cuda.synchronize()
-            timings[(r, k)] = time.perf_counter() - t0
-            eng.close()
-        r, k = min(timings, key=timings.get)
-        best[order] = {"rows": r, "depth": k}
+        timings = {r: _time_engine(group, {order: {"rows": r, "depth": 1}}, steps)
+                   for r in rows}
+        best[order] = {"rows": min(timings, key=timings.get), "depth": 1}
+    base = _time_engine(problems, best, steps)
+    for order in orders:
+        for _, k in [c for c in _candidates(order, rows, depths, problems[0].device)
+                     if c[1] > 1]:
+            trial = {o: dict(t) for o, t in best.items()}
+            trial[order]["depth"] = k
+            t = _time_engine(problems, trial, steps)
+            if t < base * (1.0 - margin):
+                best, base = trial, t
     for p in problems:
         p.reset()
     return best

@@ -980,6 +980,13 @@ struct Engine {
     int graph_steps = 0;
     size_t kernel_launches = 0;
 
+    int* words = nullptr;  // device scratch for admission results
+
+    int* scratch_words() {
+        if (!words) SB_CUDA(cudaMalloc(&words, 16 * sizeof(int)));
+        return words;
+    }
+
     Engine() {
         for (int r = 0; r <= kMaxRadius; r++) {
             tile_rows[r] = 16;
@@ -1013,8 +1020,8 @@ struct Engine {
         const size_t i = (size_t)(h.d.n - h.d.begin);
         if (blocked && !h.in_pairs) {
             if (!h.ext) {
-                SB_CUDA(cudaMalloc(&h.ext, 4 * bytes));
-                SB_CUDA(cudaMalloc(&h.pairp, sizeof(int)));
+                SB_CUDA(cudaMallocAsync(&h.ext, 4 * bytes, stream));
+                SB_CUDA(cudaMallocAsync(&h.pairp, sizeof(int), stream));
             }
             SB_CUDA(cudaMemsetAsync(h.pairp, 0, sizeof(int), stream));
             if (running) {
@@ -1066,10 +1073,11 @@ struct Engine {
                 }
                 const size_t need = h.d.rec.count * (size_t)k * win;
                 if (need > h.partial_cap) {
-                    if (h.partial) cudaFree(h.partial);
+                    if (h.partial) SB_CUDA(cudaFreeAsync(h.partial, stream));
                     h.partial = nullptr;
                     h.partial_cap = 0;
-                    SB_CUDA(cudaMalloc(&h.partial, std::max<size_t>(need, 4) * sizeof(float)));
+                    SB_CUDA(cudaMallocAsync(&h.partial, std::max<size_t>(need, 4) * sizeof(float),
+                                            stream));
                     h.partial_cap = std::max<size_t>(need, 4);
                 }
                 h.d.partial = h.partial;
@@ -1386,8 +1394,27 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
     for (size_t i = 1; i < nsteps; i++)
         chain = chain && table[3 * i] == table[3 * (i - 1) + 1] &&
                 table[3 * i + 1] == table[3 * (i - 1) + 2];
-    // window tables to the host: receivers for the tile lists, sources for
-    // the halo test
+    // engine-owned: coefficients, schedule, last-write flags (stream-ordered
+    // allocations: admission runs while other shots step)
+    SB_CUDA(cudaMallocAsync(&h.cq, 2 * (size_t)grid * sizeof(float), E.stream));
+    SB_CUDA(cudaMallocAsync(&h.slots, table.size() * sizeof(int), E.stream));
+    SB_CUDA(cudaMallocAsync(&h.keep, std::max<size_t>(nsteps, 1), E.stream));
+    SB_CUDA(cudaMemcpyAsync(h.slots, table.data(), table.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, E.stream));
+    SB_CUDA(cudaMemcpyAsync(h.keep, keep.data(), nsteps, cudaMemcpyHostToDevice, E.stream));
+    d.keep = h.keep;
+    form_coefficients(d.vel, d.damp, h.cq, h.cq + grid, grid, d.dt, E.stream);
+    SB_CUDA(cudaGetLastError());
+    // the box where Q is zero (its loads are skipped there), whether every
+    // slot's halo is zero, and the window tables (receivers for the tile
+    // lists, sources for the halo test) -- then one wait
+    int* words = E.scratch_words();
+    find_zero_box(h.cq + grid, d.L, words, E.stream);
+    SB_CUDA(cudaMemsetAsync(words + 8, 0, sizeof(int), E.stream));
+    halo_nonzero<<<256, 256, 0, E.stream>>>(d.u, d.L, (int)nsl, words + 8);
+    SB_CUDA(cudaGetLastError());
+    int box[9];
+    SB_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, E.stream));
     h.rec_iv.assign(4 * P->num_receivers, 0);
     std::vector<size_t> src_iv(4 * P->num_sources, 0);
     if (P->num_receivers)
@@ -1399,6 +1426,9 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
                                 src_iv.size() * sizeof(size_t), cudaMemcpyDeviceToHost,
                                 E.stream));
     SB_CUDA(cudaStreamSynchronize(E.stream));
+    const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
+    for (int i = 0; i < 4; i++) d.zb[i] = good ? box[i] : 0;
+    d.halo_zero = box[8] == 0;
     bool src_inside = true;
     for (size_t q = 0; q < P->num_sources; q++) {
         const size_t* b = &src_iv[4 * q];
@@ -1406,45 +1436,6 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
                      b[3] < P->nx - r;
     }
     h.blockable = !vd && chain && src_inside;
-    {
-        int* flag = nullptr;
-        SB_CUDA(cudaMalloc(&flag, sizeof(int)));
-        SB_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), E.stream));
-        halo_nonzero<<<256, 256, 0, E.stream>>>(d.u, d.L, (int)nsl, flag);
-        int nonzero = 1;
-        const cudaError_t launched = cudaGetLastError();
-        const cudaError_t copied =
-            cudaMemcpyAsync(&nonzero, flag, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
-        const cudaError_t synced = cudaStreamSynchronize(E.stream);
-        cudaFree(flag);
-        SB_CUDA(launched);
-        SB_CUDA(copied);
-        SB_CUDA(synced);
-        d.halo_zero = nonzero == 0;
-    }
-    // engine-owned: coefficients and schedule
-    SB_CUDA(cudaMalloc(&h.cq, 2 * (size_t)grid * sizeof(float)));
-    SB_CUDA(cudaMalloc(&h.slots, table.size() * sizeof(int)));
-    SB_CUDA(cudaMemcpyAsync(h.slots, table.data(), table.size() * sizeof(int),
-                            cudaMemcpyHostToDevice, E.stream));
-    SB_CUDA(cudaMalloc(&h.keep, std::max<size_t>(nsteps, 1)));
-    SB_CUDA(cudaMemcpyAsync(h.keep, keep.data(), nsteps, cudaMemcpyHostToDevice, E.stream));
-    d.keep = h.keep;
-    form_coefficients(d.vel, d.damp, h.cq, h.cq + grid, grid, d.dt, E.stream);
-    SB_CUDA(cudaGetLastError());
-    // box where Q is zero (its loads are skipped there)
-    int* words = nullptr;
-    SB_CUDA(cudaMalloc(&words, 8 * sizeof(int)));
-    find_zero_box(h.cq + grid, d.L, words, E.stream);
-    int box[7];
-    const cudaError_t copied =
-        cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, E.stream);
-    const cudaError_t synced = cudaStreamSynchronize(E.stream);
-    cudaFree(words);
-    SB_CUDA(copied);
-    SB_CUDA(synced);
-    const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
-    for (int i = 0; i < 4; i++) d.zb[i] = good ? box[i] : 0;
     d.C = h.cq;
     d.Q = h.cq + grid;
     d.slots = h.slots;
@@ -1478,13 +1469,13 @@ static void release(Engine& E, size_t i, bool restore) {
         }
         SB_CUDA(cudaGetLastError());
     }
+    cudaFreeAsync(h.cq, E.stream);
+    cudaFreeAsync(h.slots, E.stream);
+    cudaFreeAsync(h.keep, E.stream);
+    if (h.partial) cudaFreeAsync(h.partial, E.stream);
+    if (h.ext) cudaFreeAsync(h.ext, E.stream);
+    if (h.pairp) cudaFreeAsync(h.pairp, E.stream);
     SB_CUDA(cudaStreamSynchronize(E.stream));
-    cudaFree(h.cq);
-    cudaFree(h.slots);
-    cudaFree(h.keep);
-    if (h.partial) cudaFree(h.partial);
-    if (h.ext) cudaFree(h.ext);
-    if (h.pairp) cudaFree(h.pairp);
     E.shots.erase(E.shots.begin() + (long)i);
     E.dirty = true;
 }
@@ -1879,6 +1870,7 @@ extern "C" int simwave_batch_destroy(simwave_batch* b) {
         cudaFree(e->d_rec);
         cudaFree(e->d_trec);
         cudaFree(e->d_tbrec);
+        cudaFree(e->words);
         cudaStreamDestroy(e->stream);
         delete e;
     });

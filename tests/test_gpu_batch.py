@@ -261,3 +261,23 @@ def test_time_blocked_shot_released_early_resumes():
     ru, rrec, _ = oracle.forward("port", **kk)
     assert rel_l2(p.u_full_numpy(), ru) <= 1e-4
     assert rel_l2(p.shot_record_numpy(), rrec) <= 1e-4
+
+
+def test_autotune_returns_a_valid_setting():
+    from simwave_gb300.batch import BatchEngine, autotune, run_batch
+    from simwave_gb300.device import DeviceProblem
+    kws = _cd_shots(seed=40, count=4)
+    probs = [DeviceProblem(k) for k in kws]
+    tuning = autotune(probs, steps=16)
+    assert set(tuning) == {int(k["space_order"]) for k in kws}
+    for t in tuning.values():
+        assert t["rows"] in (8, 16, 32) and 1 <= t["depth"] <= 4
+    eng = BatchEngine()
+    eng.apply(tuning)
+    run_batch(probs, engine=eng)
+    eng.close()
+    for k, p in zip(kws, probs):
+        kk = dict(k, u_full=k["u_full"].copy(), shot_record=k["shot_record"].copy())
+        ru, rrec, _ = oracle.forward("port", **kk)
+        assert rel_l2(p.u_full_numpy(), ru) <= 1e-4
+        assert rel_l2(p.shot_record_numpy(), rrec) <= 1e-4
