@@ -37,6 +37,7 @@
 
 #include "simwave_gb300.h"
 #include "sw_kernels.cuh"
+#include "sw_tile2d.cuh"
 #include "sw_tiled.h"
 
 namespace sw {
@@ -113,58 +114,91 @@ __global__ void save_ring(const float* __restrict__ u, Layout L, float* __restri
     ring[t] = u[L.at2(i, j)];
 }
 
+// Transposed boundary operation of one edge (after: edge 1, before: edge 0)
+// on the line at index `line` of the other axis. `nu1` is the previous
+// adjoint level (zero halo), read for L nu^(m+1) at the halo points.
+__device__ __forceinline__ void fold_edge(float* __restrict__ nu, const float* __restrict__ nu1,
+                                          const float* __restrict__ C, const Layout& L,
+                                          const Weights<float>& W, int axis, long long line,
+                                          int edge, int type) {
+    if (type == 0) return;
+    const int r = L.r;
+    const int other = axis == 0 ? 1 : 0;
+    long long idx[2];
+    idx[other] = line;
+    idx[axis] = edge ? L.extent(axis) - r - 1 : r;
+    const long long first = L.at2(idx[0], idx[1]);
+    if (type == 1) {
+        nu[first] = 0.0f;
+        return;
+    }
+    // Neumann: halo a = first + dir q step mirrors b = first - dir q step
+    const long long step = L.stride(axis);
+    const float ih2 = W.ih2[axis];
+    const long long inward = edge ? -step : step;
+    for (int q = 1; q <= r; q++) {
+        float lam = 0.0f;
+        for (int k = q; k <= r; k++) lam += W.c2[k] * nu1[first + (k - q) * inward];
+        const long long b = first + q * inward;
+        nu[b] += C[b] * (lam * ih2);
+    }
+}
+
 // Transposed boundary operations of the edges normal to `axis`, one thread
 // per line: the after edge, then the before edge (the forward applies them
-// in the opposite order; they touch disjoint points). `nu1` is the previous
-// adjoint level (zero halo), read for L nu^(m+1) at the halo points.
+// in the opposite order; they touch disjoint points).
 __global__ void fold_phase(float* __restrict__ nu, const float* __restrict__ nu1,
                            const float* __restrict__ C, Layout L, Weights<float> W, int axis,
                            int before, int after) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= boundary_lines(L, axis)) return;
-    const int r = L.r;
-    const int other = axis == 0 ? 1 : 0;
-    long long idx[2];
-    idx[other] = r + t;
-    const long long step = L.stride(axis);
-    const float ih2 = W.ih2[axis];
-    for (int edge = 1; edge >= 0; edge--) {
-        const int type = edge ? after : before;
-        if (type == 0) continue;
-        idx[axis] = edge ? L.extent(axis) - r - 1 : r;
-        const long long first = L.at2(idx[0], idx[1]);
-        if (type == 1) {
-            nu[first] = 0.0f;
-            continue;
-        }
-        // Neumann: halo a = first + dir q step mirrors b = first - dir q step
-        const long long inward = edge ? -step : step;
-        for (int q = 1; q <= r; q++) {
-            float lam = 0.0f;
-            for (int k = q; k <= r; k++) lam += W.c2[k] * nu1[first + (k - q) * inward];
-            const long long b = first + q * inward;
-            nu[b] += C[b] * (lam * ih2);
-        }
-    }
+    fold_edge(nu, nu1, C, L, W, axis, L.r + t, 1, after);
+    fold_edge(nu, nu1, C, L, W, axis, L.r + t, 0, before);
 }
 
-// Receiver transposes, gathered per grid point in receiver order (no
-// atomics, so the sum order is fixed): nu[p] += C[p] * sum_e wt[e] g[rec[e]].
-__global__ void adjoint_receivers(float* __restrict__ nu, const float* __restrict__ C,
-                                  const long long* __restrict__ pts,
-                                  const int* __restrict__ rowptr, const int* __restrict__ rec,
-                                  const float* __restrict__ wt,
-                                  const float* __restrict__ g_row, int npts) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= npts) return;
+// Receiver transposes of table point t (receiver order within the point,
+// no atomics, so the sum order is fixed): nu[p] += C[p] * sum_e wt[e] g[rec[e]].
+__device__ __forceinline__ void inject_point(float* __restrict__ nu, const float* __restrict__ C,
+                                             const long long* __restrict__ pts,
+                                             const int* __restrict__ rowptr,
+                                             const int* __restrict__ rec,
+                                             const float* __restrict__ wt,
+                                             const float* __restrict__ g_row, int t) {
     float s = 0.0f;
     for (int e = rowptr[t]; e < rowptr[t + 1]; e++) s += wt[e] * g_row[rec[e]];
     const long long p = pts[t];
     nu[p] += C[p] * s;
 }
 
-// grad += nu^m K (w^m - 2 u^(m-1) + u^(m-2)) over the interior; w^m comes
-// from the saved ring where `ring` is set.
+__global__ void adjoint_receivers(float* __restrict__ nu, const float* __restrict__ C,
+                                  const long long* __restrict__ pts,
+                                  const int* __restrict__ rowptr, const int* __restrict__ rec,
+                                  const float* __restrict__ wt,
+                                  const float* __restrict__ g_row, int npts) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < npts) inject_point(nu, C, pts, rowptr, rec, wt, g_row, t);
+}
+
+// grad += nu^m K (w^m - 2 u^(m-1) + u^(m-2)) at interior point (i, j); w^m
+// comes from the saved ring where `ring` is set.
+__device__ __forceinline__ void accumulate_point(float* __restrict__ grad,
+                                                 const float* __restrict__ nu,
+                                                 const float* __restrict__ u_m,
+                                                 const float* __restrict__ u_m1,
+                                                 const float* __restrict__ u_m2,
+                                                 const float* __restrict__ K,
+                                                 const float* __restrict__ ring, const Layout& L,
+                                                 long long i, long long j) {
+    const long long p = L.at2(i, j);
+    float w = u_m[p];
+    if (ring) {
+        const long long ri = ring_index(L, i, j);
+        if (ri >= 0) w = ring[ri];
+    }
+    const float d2 = (w - 2.0f * u_m1[p]) + u_m2[p];
+    grad[p] += nu[p] * K[p] * d2;
+}
+
 __global__ void accumulate_gradient(float* __restrict__ grad, const float* __restrict__ nu,
                                     const float* __restrict__ u_m,
                                     const float* __restrict__ u_m1,
@@ -175,14 +209,101 @@ __global__ void accumulate_gradient(float* __restrict__ grad, const float* __res
     const long long j = r + blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long i = r + blockIdx.y * (long long)blockDim.y + threadIdx.y;
     if (j >= L.nx - r || i >= L.nz - r) return;
-    const long long p = L.at2(i, j);
-    float w = u_m[p];
-    if (ring) {
-        const long long ri = ring_index(L, i, j);
-        if (ri >= 0) w = ring[ri];
+    accumulate_point(grad, nu, u_m, u_m1, u_m2, K, ring, L, i, j);
+}
+
+// ---- one adjoint step in one launch -----------------------------------------
+// Tiles of 16 x 128 interior points, as in the forward's tiled kernel. A CTA
+// computes the stencil on nu for its tile, then, for the points it owns, the
+// receiver transposes (the table is tile-major), the transposed z edges, the
+// transposed x edges and the gradient terms -- the separate kernels' order,
+// exact when the first and last tiles hold r + 1 rows and columns (an
+// edge's fold reaches r points in from the edge line).
+struct AdjointTiles {
+    Layout L;
+    const float *C, *Q, *K;
+    Weights<float> W;
+    int zb[4];
+    int bc[4];
+    int tiles_x, tiles_z;
+    const long long* pts;
+    const int *rowptr, *rec, *tile_ptr;
+    const float* wt;
+    float* grad;
+};
+
+extern __shared__ __align__(16) float4 sw_grad_smem[];
+
+template <int R>
+__global__ void __launch_bounds__(batch::kThreads)
+adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* nu2,
+               const float* g_row, const float* u_m, const float* u_m1, const float* u_m2,
+               const float* ring) {
+    const int t = blockIdx.x;
+    const int tz = t / A.tiles_x, tx = t - (t / A.tiles_x) * A.tiles_x;
+    const Layout& L = A.L;
+    batch::stencil2d_tile<R, false, 16>(reinterpret_cast<float*>(sw_grad_smem), L, num, nu1,
+                                        nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx);
+    __syncthreads();
+    if (A.pts)
+        for (int e = A.tile_ptr[t] + threadIdx.x; e < A.tile_ptr[t + 1]; e += blockDim.x)
+            inject_point(num, A.C, A.pts, A.rowptr, A.rec, A.wt, g_row, e);
+    __syncthreads();
+    const int nz = (int)L.nz, nx = (int)L.nx;
+    const int z0 = R + 16 * tz, z1 = min(z0 + 16, nz - R);
+    const int x0 = R + 128 * tx, x1 = min(x0 + 128, nx - R);
+    // transposed order: z edges (the columns of this tile), then x edges
+    if ((tz == A.tiles_z - 1 && A.bc[1]) || (tz == 0 && A.bc[0])) {
+        for (int c = x0 + threadIdx.x; c < x1; c += blockDim.x) {
+            if (tz == A.tiles_z - 1) fold_edge(num, nu1, A.C, L, A.W, 0, c, 1, A.bc[1]);
+            if (tz == 0) fold_edge(num, nu1, A.C, L, A.W, 0, c, 0, A.bc[0]);
+        }
     }
-    const float d2 = (w - 2.0f * u_m1[p]) + u_m2[p];
-    grad[p] += nu[p] * K[p] * d2;
+    __syncthreads();
+    if ((tx == A.tiles_x - 1 && A.bc[3]) || (tx == 0 && A.bc[2])) {
+        for (int i = z0 + threadIdx.x; i < z1; i += blockDim.x) {
+            if (tx == A.tiles_x - 1) fold_edge(num, nu1, A.C, L, A.W, 1, i, 1, A.bc[3]);
+            if (tx == 0) fold_edge(num, nu1, A.C, L, A.W, 1, i, 0, A.bc[2]);
+        }
+    }
+    __syncthreads();
+    const int w = x1 - x0;
+    for (int q = threadIdx.x; q < (z1 - z0) * w; q += blockDim.x) {
+        const int i = z0 + q / w, j = x0 + q % w;
+        accumulate_point(A.grad, num, u_m, u_m1, u_m2, A.K, ring, L, i, j);
+    }
+}
+
+template <int R>
+static void adjoint_r(const AdjointTiles& A, float* num, const float* nu1, const float* nu2,
+                      const float* g_row, const float* u_m, const float* u_m1,
+                      const float* u_m2, const float* ring, cudaStream_t st) {
+    constexpr int HX = (R + 3) & ~3;
+    const int bytes = (16 + 2 * R) * (128 + 2 * HX) * 4;
+    static bool configured[64] = {};
+    int dev = 0;
+    GR_CUDA(cudaGetDevice(&dev));
+    if (!configured[dev & 63]) {
+        GR_CUDA(cudaFuncSetAttribute(adjoint2d_step<R>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        configured[dev & 63] = true;
+    }
+    adjoint2d_step<R><<<A.tiles_x * A.tiles_z, batch::kThreads, bytes, st>>>(
+        A, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring);
+}
+
+static void adjoint_launch(const AdjointTiles& A, float* num, const float* nu1,
+                           const float* nu2, const float* g_row, const float* u_m,
+                           const float* u_m1, const float* u_m2, const float* ring,
+                           cudaStream_t st) {
+#define GR_A(RR)                                                                        \
+    case RR:                                                                            \
+        adjoint_r<RR>(A, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring, st);              \
+        break;
+    switch (A.L.r) {
+        GR_A(1) GR_A(2) GR_A(3) GR_A(4) GR_A(5) GR_A(6) GR_A(7) GR_A(8) GR_A(9) GR_A(10)
+    }
+#undef GR_A
 }
 
 // ---------------------------------------------------------------------------
@@ -452,12 +573,15 @@ static void forward_pass(const simwave_problem* P, size_t interval, float* ck,
     }
 }
 
-// Receiver transposes as a point-major table (receiver order within a point).
+// Receiver transposes as a point-major table (receiver order within a
+// point), points grouped by the 16 x 128 interior tile that holds them
+// (`tile_ptr`: each tile's range) and in grid order within a tile.
 struct AdjointTable {
     long long* pts = nullptr;
     int* rowptr = nullptr;
     int* rec = nullptr;
     float* wt = nullptr;
+    int* tile_ptr = nullptr;
     int npts = 0;
 };
 
@@ -467,6 +591,15 @@ static AdjointTable build_table(const HostWindows& H, size_t count, const Layout
         long long p;
         int s;
         float w;
+        int tile;
+    };
+    const int r = L.r;
+    const int tiles_x = (int)((L.nx - 2 * r + 127) / 128);
+    const int tiles_z = (int)((L.nz - 2 * r + 15) / 16);
+    auto tile_of = [&](long long z, long long x) {
+        const long long tz = std::min<long long>(std::max<long long>(z - r, 0) / 16, tiles_z - 1);
+        const long long tx = std::min<long long>(std::max<long long>(x - r, 0) / 128, tiles_x - 1);
+        return (int)(tz * tiles_x + tx);
     };
     std::vector<Entry> e;
     for (size_t s = 0; s < count; s++) {
@@ -477,24 +610,32 @@ static AdjointTable build_table(const HostWindows& H, size_t count, const Layout
         for (size_t iz = 0; iz < lz; iz++)
             for (size_t ix = 0; ix < lx; ix++)
                 e.push_back({L.at2((long long)(b[0] + iz), (long long)(b[2] + ix)), (int)s,
-                             kz[iz] * kx[ix]});
+                             kz[iz] * kx[ix],
+                             tile_of((long long)(b[0] + iz), (long long)(b[2] + ix))});
     }
-    std::stable_sort(e.begin(), e.end(), [](const Entry& a, const Entry& b) { return a.p < b.p; });
+    std::stable_sort(e.begin(), e.end(), [](const Entry& a, const Entry& b) {
+        return a.tile != b.tile ? a.tile < b.tile : a.p < b.p;
+    });
     std::vector<long long> pts;
-    std::vector<int> rowptr{0}, rec;
+    std::vector<int> rowptr{0}, rec, tile_ptr(tiles_x * tiles_z + 1, 0);
     std::vector<float> wt;
     for (size_t k = 0; k < e.size(); k++) {
         if (k == 0 || e[k].p != e[k - 1].p) {
             if (k) rowptr.push_back((int)rec.size());
             pts.push_back(e[k].p);
+            tile_ptr[e[k].tile + 1]++;
         }
         rec.push_back(e[k].s);
         wt.push_back(e[k].w);
     }
     if (!e.empty()) rowptr.push_back((int)rec.size());
+    for (size_t t = 1; t < tile_ptr.size(); t++) tile_ptr[t] += tile_ptr[t - 1];
     AdjointTable T;
     T.npts = (int)pts.size();
     if (!T.npts) return T;
+    T.tile_ptr = mem.get<int>(tile_ptr.size());
+    GR_CUDA(cudaMemcpyAsync(T.tile_ptr, tile_ptr.data(), tile_ptr.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, mem.st));
     T.pts = mem.get<long long>(pts.size());
     T.rowptr = mem.get<int>(rowptr.size());
     T.rec = mem.get<int>(rec.size());
@@ -535,6 +676,26 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
     gradient_factor<<<1024, 256, 0, st>>>(X.vel, Kf, (long long)G, X.dt);
     GR_LAUNCHED("gradient_factor");
     const AdjointTable T = build_table(R, P->num_receivers, X.L, mem);
+    AdjointTiles A{};
+    if (X.fused) {
+        A.L = X.L;
+        A.C = X.C;
+        A.Q = X.Q;
+        A.K = Kf;
+        A.W = X.W;
+        for (int i = 0; i < 4; i++) {
+            A.zb[i] = X.zero_box[i];
+            A.bc[i] = X.bc[i];
+        }
+        A.tiles_x = X.shot.tiles_x;
+        A.tiles_z = X.shot.tiles_z;
+        A.pts = T.npts ? T.pts : nullptr;
+        A.rowptr = T.rowptr;
+        A.rec = T.rec;
+        A.wt = T.wt;
+        A.tile_ptr = T.tile_ptr;
+        A.grad = grad;
+    }
 
     const int r = X.L.r;
     const dim3 gblock(32, 8, 1);
@@ -557,6 +718,14 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
             float* num = nu + (m % 3) * G;
             const float* nu1 = nu + ((m + 1) % 3) * G;
             const float* nu2 = nu + ((m + 2) % 3) * G;
+            if (X.fused) {  // the whole adjoint step in one launch
+                const size_t k = m - n0;
+                adjoint_launch(A, num, nu1, nu2, g + (m - 1) * P->num_receivers,
+                               seg + (k + 1) * G, seg + k * G, seg + (k - 1) * G,
+                               ring ? ring + (m - 1 - n0) * (size_t)ring_len : nullptr, st);
+                GR_LAUNCHED("adjoint2d_step");
+                continue;
+            }
             stencil(X, num, nu1, nu2, st);
             if (T.npts) {
                 adjoint_receivers<<<(unsigned)((T.npts + 255) / 256), 256, 0, st>>>(
