@@ -276,6 +276,16 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
     const bool edge = zr0 <= R || zr0 + TH > nz - R - 1 || xc0 <= R || xc0 + TW > nx - R - 1;
     const bool reload = edge && !S.halo_zero;
     const int bz0 = S.bc[0], bz1 = S.bc[1], bx0 = S.bc[2], bx1 = S.bc[3];
+    // descriptor fields the loops read, held in registers (the shared-memory
+    // accesses are compiler barriers: fields read through S would be
+    // re-fetched from global memory on every row)
+    const int zbox0 = S.zb[0], zbox1 = S.zb[1];
+    float* const partial = S.partial;
+    const int win = S.win;
+    const unsigned char* const keep = S.keep + (n0 - S.begin);
+    const int* const next_slot = S.slots + 3 * (n0 - S.begin) + 2;
+    float* const u0 = S.u;
+    const long long slot = L.slot;
     __syncthreads();
     if (kk == 1)  // the block's last two levels: the staged u_cur and the one it computes
         tb_copy_owned(U, S.ext + (long long)(2 * (pair ^ 1)) * S.grid, TW, zr0, xc0, zlo, zhi,
@@ -287,7 +297,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
             const TbRec q = trec[t.rec_first + e];
             const int w = q.x1 - q.x0;
             const int cnt = (q.z1 - q.z0) * w;
-            float* dst = S.partial + ((size_t)q.rc * K + j) * S.win;
+            float* dst = partial + ((size_t)q.rc * K + j) * win;
             for (int i = lane; i < cnt; i += 32) {
                 const int z = q.z0 + i / w, xx = q.x0 + i % w;
                 dst[(z - q.b0) * q.lx + (xx - q.b2)] = U[(z - zr0) * TW + (xx - xc0)];
@@ -298,7 +308,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
         for (int rr = rlo + warp; rr < rhi; rr += kTbWarps) {
             const int z = zr0 + rr;
             if (z < R || z >= nz - R || !xany) continue;
-            const bool qzero = xbox && z >= S.zb[0] && z < S.zb[1];
+            const bool qzero = xbox && z >= zbox0 && z < zbox1;
             const V4 cc = lds_v4(Cs + (rr - R) * 128 + 4 * lane);
             const V4 qq = lds_v4(Qs + (rr - R) * 128 + 4 * lane);
             const float* tu = U + rr * TW + 4 * lane;
@@ -350,7 +360,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
             }
         }
         __syncthreads();
-        float* un = S.u + (long long)S.slots[3 * (n - S.begin) + 2] * L.slot;
+        float* un = u0 + (long long)next_slot[3 * j] * slot;
         if (reload) {
             // halo points of the new level: what its slot holds (the per-step
             // kernels never write them before the boundary phases); halo rows
@@ -460,7 +470,7 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
         if (j >= kk - 2)
             tb_copy_owned(P, S.ext + (long long)(2 * (pair ^ 1) + (j - (kk - 2))) * S.grid, TW,
                           zr0, xc0, zlo, zhi, xlo, xhi, pitch, lead, warp, lane);
-        if (S.keep[n - S.begin]) {
+        if (keep[j]) {
             const int xa = xlo - ((lead + xlo) & 3);  // 16-byte aligned start
             const int nch = (xhi - xa + 3) / 4;
             for (int zz = zlo + warp; zz < zhi; zz += kTbWarps) {
