@@ -3,18 +3,21 @@
 // A shot is one forward problem (2D, float32, any order, density and saving
 // stride) whose arrays are resident on the device (the caller owns u, the
 // models, the KWS tables, the wavelet and the receivers; the engine owns the
-// per-point coefficients C, Q and the shot's slot schedule). Each time step of
-// the batch is a fixed sequence of launches over *all* shots:
-//   1. stencil   one launch per (radius, density) group; a CTA is one
-//                128 x TZ tile of one shot (tile list in device memory)
-//   2. sources   one block per (shot, source)
-//   3. x edges, then z edges (the reference's order), one block per shot
-//   4. receivers one warp per (shot, receiver)
-//   5. advance   each shot's step counter
-// Every kernel reads the shot's current step from its device descriptor and
-// does nothing for a shot that is past its last step, so the launch sequence
-// of K steps is captured once into a CUDA graph and replayed until the set of
-// shots changes (shots that finish simply go idle).
+// per-point coefficients C, Q and the shot's slot schedule). Each launch
+// round of the batch is a fixed sequence of launches over *all* shots:
+//   1. stencil   one launch per (radius, density, depth) group; a CTA is one
+//                128 x TZ tile of one shot (tile list in device memory), or,
+//                for time-blocked groups, one tile advanced `depth` steps
+//                with its sources, edges and receiver copies
+//   2. sources   one block per (shot, source)            } per-step shots
+//   3. x edges, then z edges (the reference's order)     } only
+//   4. receivers one warp per (shot, receiver); the time-blocked shots'
+//                records are summed from their window copies
+//   5. advance   each shot's step counter (by 1 or by its block)
+// Every kernel reads the shot's current step and the run's stop step from
+// its device descriptor and does nothing for a shot past them, so the
+// sequence of 16 rounds is captured once into a CUDA graph and replayed
+// until the set of shots changes (shots that finish simply go idle).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,7 +40,6 @@ void record_error(const std::string& message);
 
 namespace batch {
 
-constexpr int kMaxGroups = 2 * kMaxRadius;  // (radius, density) pairs
 
 // Device descriptor of one shot.
 struct Shot {
