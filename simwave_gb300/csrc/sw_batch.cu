@@ -81,7 +81,8 @@ struct ZeroBox2 {
 
 struct TileRef {
     int shot, tz, tx;
-    int rec_first, rec_count;  // time-blocked tiles: their (receiver, slot) entries
+    int rec_first, rec_count;  // time-blocked tiles: their receiver-window parts
+    int src_first, src_count;  // time-blocked tiles: sources whose window meets the region
 };
 struct PairRef {
     int shot, item;
@@ -209,7 +210,7 @@ __device__ __forceinline__ void tb_copy_owned(const float* buf, float* g, int tw
 template <int R, int K>
 __global__ void __launch_bounds__(kTbThreads, 1)
 stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ tiles,
-                 const TbRec* __restrict__ trec) {
+                 const TbRec* __restrict__ trec, const int* __restrict__ tsrc) {
     constexpr int HX = (R + 3) & ~3;
     constexpr int TW = 128 + 2 * HX;
     constexpr int TH = kTbRows;
@@ -288,10 +289,17 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
     const int* const next_slot = S.slots + 3 * (n0 - S.begin) + 2;
     float* const u0 = S.u;
     const long long slot = L.slot;
+    float* const ext_out = S.ext + (long long)(2 * (pair ^ 1)) * S.grid;
+    const long long grid = S.grid;
+    const Windows<float> src = S.src;
+    const float* const wavelet = S.wavelet;
+    const size_t wcount = (size_t)S.wavelet_count;
+    const float* const vel = S.vel;
+    const float* const damp = S.damp;
+    const float dt = S.dt, dt2 = S.dt2;
     __syncthreads();
     if (kk == 1)  // the block's last two levels: the staged u_cur and the one it computes
-        tb_copy_owned(U, S.ext + (long long)(2 * (pair ^ 1)) * S.grid, TW, zr0, xc0, zlo, zhi,
-                      xlo, xhi, pitch, lead, warp, lane);
+        tb_copy_owned(U, ext_out, TW, zr0, xc0, zlo, zhi, xlo, xhi, pitch, lead, warp, lane);
     for (int j = 0; j < kk; j++) {
         const int n = n0 + j;
         // receivers: this tile's part of each window of level n, to scratch
@@ -392,27 +400,23 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
             }
             __syncthreads();
         }
-        if (S.src.count) {
-            const float dt2 = S.dt2;
-            for (size_t s = 0; s < S.src.count; s++) {
-                const float w = wavelet_at(S.wavelet, (size_t)S.wavelet_count, (size_t)n,
-                                           S.src.count, s);
+        if (t.src_count) {
+            for (int q = 0; q < t.src_count; q++) {
+                const size_t s = (size_t)tsrc[t.src_first + q];
+                const float w = wavelet_at(wavelet, wcount, (size_t)n, src.count, s);
                 if (w == 0.f) continue;
-                const size_t* b = S.src.interval + 4 * s;
-                if ((int)b[1] < zr0 || (int)b[0] >= zr0 + TH || (int)b[3] < xc0 ||
-                    (int)b[2] >= xc0 + TW)
-                    continue;
-                const float* v = S.src.values + S.src.offsets[s];
+                const size_t* b = src.interval + 4 * s;
+                const float* v = src.values + src.offsets[s];
                 const long long total = window_size<2>(b);
-                for (long long q = threadIdx.x; q < total; q += kTbThreads) {
+                for (long long i = threadIdx.x; i < total; i += kTbThreads) {
                     long long iz, ix, iy;
-                    window_point<2>(b, q, iz, ix, iy);
+                    window_point<2>(b, i, iz, ix, iy);
                     const int z = (int)(b[0] + iz), xx = (int)(b[2] + ix);
                     if (z < zr0 || z >= zr0 + TH || xx < xc0 || xx >= xc0 + TW) continue;
                     const float kws = window_weight<float, 2>(b, v, iz, ix, iy);
                     const long long p = L.at2(z, xx);
-                    const float vv = S.vel[p] * S.vel[p];
-                    const float d = 1.f + S.damp[p] * S.dt * vv * 0.5f;
+                    const float vv = vel[p] * vel[p];
+                    const float d = 1.f + damp[p] * dt * vv * 0.5f;
                     atomicAdd(P + (z - zr0) * TW + (xx - xc0), dt2 * vv * kws * w / d);
                 }
             }
@@ -470,8 +474,8 @@ stencil2d_tblock(const Shot* __restrict__ shots, const TileRef* __restrict__ til
         // write it (interior and Neumann mirrors), when that is the slot's
         // last write
         if (j >= kk - 2)
-            tb_copy_owned(P, S.ext + (long long)(2 * (pair ^ 1) + (j - (kk - 2))) * S.grid, TW,
-                          zr0, xc0, zlo, zhi, xlo, xhi, pitch, lead, warp, lane);
+            tb_copy_owned(P, ext_out + (j - (kk - 2)) * grid, TW, zr0, xc0, zlo, zhi, xlo, xhi,
+                          pitch, lead, warp, lane);
         if (keep[j]) {
             const int xa = xlo - ((lead + xlo) & 3);  // 16-byte aligned start
             const int nch = (xhi - xa + 3) / 4;
@@ -673,6 +677,7 @@ struct HostShot {
     std::vector<int> perm;   // final logical -> physical slots
     std::vector<int> table;  // per step: prev, cur, next physical slots
     std::vector<size_t> rec_iv;  // receiver windows (host copy)
+    std::vector<size_t> src_iv;  // source windows (host copy)
     float* ext = nullptr;    // engine-owned level pairs (time-blocked)
     int* pairp = nullptr;
     bool in_pairs = false;   // the latest levels live in `ext`, not the slots
@@ -727,7 +732,7 @@ static void launch_group_r(bool configure, int tz, const Shot* shots, const Tile
 
 template <int R, int K>
 static void launch_tblock_t(bool configure, const Shot* shots, const TileRef* tiles,
-                            const TbRec* trec, int ntiles, cudaStream_t st) {
+                            const TbRec* trec, const int* tsrc, int ntiles, cudaStream_t st) {
     if constexpr (tb_supported(R, K)) {
         constexpr int HX = (R + 3) & ~3;
         const int bytes = (2 * kTbRows * (128 + 2 * HX) + 2 * (kTbRows - 2 * R) * 128) * 4;
@@ -736,7 +741,7 @@ static void launch_tblock_t(bool configure, const Shot* shots, const TileRef* ti
                                  bytes);
             return;
         }
-        stencil2d_tblock<R, K><<<ntiles, kTbThreads, bytes, st>>>(shots, tiles, trec);
+        stencil2d_tblock<R, K><<<ntiles, kTbThreads, bytes, st>>>(shots, tiles, trec, tsrc);
     } else {
         fail(SIMWAVE_E_ARGUMENT, "time-block depth too large for the space order");
     }
@@ -744,17 +749,17 @@ static void launch_tblock_t(bool configure, const Shot* shots, const TileRef* ti
 
 template <int R>
 static void launch_tblock_r(bool configure, int k, const Shot* shots, const TileRef* tiles,
-                            const TbRec* trec, int ntiles, cudaStream_t st) {
-    if (k == 2) launch_tblock_t<R, 2>(configure, shots, tiles, trec, ntiles, st);
-    else if (k == 3) launch_tblock_t<R, 3>(configure, shots, tiles, trec, ntiles, st);
-    else launch_tblock_t<R, 4>(configure, shots, tiles, trec, ntiles, st);
+                            const TbRec* trec, const int* tsrc, int ntiles, cudaStream_t st) {
+    if (k == 2) launch_tblock_t<R, 2>(configure, shots, tiles, trec, tsrc, ntiles, st);
+    else if (k == 3) launch_tblock_t<R, 3>(configure, shots, tiles, trec, tsrc, ntiles, st);
+    else launch_tblock_t<R, 4>(configure, shots, tiles, trec, tsrc, ntiles, st);
 }
 
 static void launch_tblock(bool configure, int r, int k, const Shot* shots, const TileRef* tiles,
-                          const TbRec* trec, int ntiles, cudaStream_t st) {
+                          const TbRec* trec, const int* tsrc, int ntiles, cudaStream_t st) {
 #define SB_T(RR)                                                                          \
     case RR:                                                                              \
-        launch_tblock_r<RR>(configure, k, shots, tiles, trec, ntiles, st);                \
+        launch_tblock_r<RR>(configure, k, shots, tiles, trec, tsrc, ntiles, st);          \
         break;
     switch (r) {
         SB_T(1) SB_T(2) SB_T(3) SB_T(4) SB_T(5) SB_T(6) SB_T(7) SB_T(8) SB_T(9) SB_T(10)
@@ -814,6 +819,8 @@ struct Engine {
     size_t cap_trec = 0;
     PairRef* d_tbrec = nullptr;  // receivers of time-blocked shots
     size_t cap_tbrec = 0;
+    int* d_tsrc = nullptr;       // sources meeting each time-blocked tile's region
+    size_t cap_tsrc = 0;
     struct Group {
         int r;
         bool vd;
@@ -906,6 +913,7 @@ struct Engine {
         std::map<std::tuple<int, int, int>, std::vector<TileRef>> byg;
         std::vector<PairRef> srcp, recp, tbrecp;
         std::vector<TbRec> trec;
+        std::vector<int> tsrc;
         any_stepwise = false;
         for (size_t i = 0; i < ns; i++) {
             HostShot& h = shots[i];
@@ -962,10 +970,22 @@ struct Engine {
                     tbrecp.push_back({(int)i, (int)q});
                 }
                 auto& v = byg[{r, 0, k}];
+                const int hx = (r + 3) & ~3;
                 for (int a = 0; a < nt_z; a++)
                     for (int c = 0; c < nt_x; c++) {
                         const auto& e = per[a * nt_x + c];
-                        v.push_back({(int)i, a, c, (int)trec.size(), (int)e.size()});
+                        // the staged region: kTbRows rows from zr0, 128 + 2 hx columns from xc0
+                        const long long zr0 = r + (long long)a * g.oz - g.mz;
+                        const long long xc0 = r + (long long)c * g.ox - g.dx - hx;
+                        const int first_src = (int)tsrc.size();
+                        for (size_t q = 0; q < h.d.src.count; q++) {
+                            const size_t* b = &h.src_iv[4 * q];
+                            if ((long long)b[1] >= zr0 && (long long)b[0] < zr0 + kTbRows &&
+                                (long long)b[3] >= xc0 && (long long)b[2] < xc0 + 128 + 2 * hx)
+                                tsrc.push_back((int)q);
+                        }
+                        v.push_back({(int)i, a, c, (int)trec.size(), (int)e.size(), first_src,
+                                     (int)tsrc.size() - first_src});
                         trec.insert(trec.end(), e.begin(), e.end());
                     }
             } else {
@@ -975,7 +995,7 @@ struct Engine {
                 const int nt_x = (int)((L.nx - 2 * r + 127) / 128);
                 auto& v = byg[{r, h.d.den ? 1 : 0, 1}];
                 for (int a = 0; a < nt_z; a++)
-                    for (int b = 0; b < nt_x; b++) v.push_back({(int)i, a, b, 0, 0});
+                    for (int b = 0; b < nt_x; b++) v.push_back({(int)i, a, b, 0, 0, 0, 0});
                 for (size_t q = 0; q < h.d.src.count; q++) srcp.push_back({(int)i, (int)q});
                 for (size_t q = 0; q < h.d.rec.count; q++) recp.push_back({(int)i, (int)q});
             }
@@ -993,6 +1013,7 @@ struct Engine {
         grow(d_rec, cap_rec, recp.size());
         grow(d_trec, cap_trec, trec.size());
         grow(d_tbrec, cap_tbrec, tbrecp.size());
+        grow(d_tsrc, cap_tsrc, tsrc.size());
         if (ns) SB_CUDA(cudaMemcpyAsync(d_shots, desc.data(), ns * sizeof(Shot),
                                         cudaMemcpyHostToDevice, stream));
         if (!all.empty())
@@ -1010,13 +1031,16 @@ struct Engine {
         if (!tbrecp.empty())
             SB_CUDA(cudaMemcpyAsync(d_tbrec, tbrecp.data(), tbrecp.size() * sizeof(PairRef),
                                     cudaMemcpyHostToDevice, stream));
+        if (!tsrc.empty())
+            SB_CUDA(cudaMemcpyAsync(d_tsrc, tsrc.data(), tsrc.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, stream));
         SB_CUDA(cudaStreamSynchronize(stream));
         nsrc_pairs = (int)srcp.size();
         nrec_pairs = (int)recp.size();
         ntb_rec = (int)tbrecp.size();
         for (const Group& g : groups) {
             if (g.depth > 1)
-                launch_tblock(true, g.r, g.depth, nullptr, nullptr, nullptr, 0, stream);
+                launch_tblock(true, g.r, g.depth, nullptr, nullptr, nullptr, nullptr, 0, stream);
             else
                 launch_group(true, g.r, g.vd, tile_rows[g.r], nullptr, nullptr, 0, stream);
         }
@@ -1035,8 +1059,8 @@ struct Engine {
     void enqueue_step(cudaStream_t st) {
         for (const Group& g : groups) {
             if (g.depth > 1)
-                launch_tblock(false, g.r, g.depth, d_shots, d_tiles + g.first, d_trec, g.count,
-                              st);
+                launch_tblock(false, g.r, g.depth, d_shots, d_tiles + g.first, d_trec, d_tsrc,
+                              g.count, st);
             else
                 launch_group(false, g.r, g.vd, tile_rows[g.r], d_shots, d_tiles + g.first,
                              g.count, st);
@@ -1265,7 +1289,8 @@ static void admit(Engine& E, const simwave_problem* P, int* id) {
     int box[9];
     SB_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, E.stream));
     h.rec_iv.assign(4 * P->num_receivers, 0);
-    std::vector<size_t> src_iv(4 * P->num_sources, 0);
+    h.src_iv.assign(4 * P->num_sources, 0);
+    std::vector<size_t>& src_iv = h.src_iv;
     if (P->num_receivers)
         SB_CUDA(cudaMemcpyAsync(h.rec_iv.data(), P->rec_points_interval,
                                 h.rec_iv.size() * sizeof(size_t), cudaMemcpyDeviceToHost,
@@ -1719,6 +1744,7 @@ extern "C" int simwave_batch_destroy(simwave_batch* b) {
         cudaFree(e->d_rec);
         cudaFree(e->d_trec);
         cudaFree(e->d_tbrec);
+        cudaFree(e->d_tsrc);
         cudaFree(e->words);
         cudaStreamDestroy(e->stream);
         delete e;
