@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -787,7 +788,7 @@ static void single_r(const Layout& L, float* un, const float* uc, const float* u
                      const Weights<float>& W, const int* box, cudaStream_t st) {
     constexpr int TZ = 16, HX = (R + 3) & ~3;
     const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (!configured[dev & 63]) {
@@ -1586,7 +1587,7 @@ static void step_r(const Shot2D& P, float* un, const float* uc, const float* up,
     constexpr int TZ = 16;
     constexpr int HX = (R + 3) & ~3;
     const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     SB_CUDA(cudaGetDevice(&dev));
     if (!configured[dev & 63]) {
@@ -1605,7 +1606,7 @@ static bool persistent_r(const Persist2D& P, cudaStream_t st) {
     constexpr int HX = (R + 3) & ~3;
     const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
     auto kernel = stencil2d_persistent<R, VD, TZ>;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     SB_CUDA(cudaGetDevice(&dev));
     if (!configured[dev & 63]) {

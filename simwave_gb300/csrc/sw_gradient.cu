@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -280,7 +281,7 @@ static void adjoint_r(const AdjointTiles& A, float* num, const float* nu1, const
                       const float* u_m2, const float* ring, cudaStream_t st) {
     constexpr int HX = (R + 3) & ~3;
     const int bytes = (16 + 2 * R) * (128 + 2 * HX) * 4;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     GR_CUDA(cudaGetDevice(&dev));
     if (!configured[dev & 63]) {

@@ -22,6 +22,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1017,7 +1018,7 @@ void launch_r(float* un, const float* uc, const float* up, const float* vel, con
               const float* damp, const Layout& L, const Weights<float>& W, float dt, float dt2,
               const TiledContext& ctx, cudaStream_t st) {
     using TL = Tile<R>;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     cudaGetDevice(&dev);
     const size_t smem = smem_bytes<R, VD>();
@@ -1029,7 +1030,7 @@ void launch_r(float* un, const float* uc, const float* up, const float* vel, con
     const int ty = (int)((L.ny - 2 * R + 31) / 32);
     const int tx = (int)((L.nx - 2 * R + TL::TX - 1) / TL::TX);
     const int nzi = (int)(L.nz - 2 * R);
-    static int per_sm_of[64] = {};  // resident CTAs per SM, queried once per device
+    static std::atomic<int> per_sm_of[64];  // resident CTAs per SM, queried once per device
     if (!per_sm_of[dev & 63]) {
         int v = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, stencil3d_tiled<R, VD>, kThreads, smem);
@@ -1100,7 +1101,7 @@ void launch_vec(float* un, const float* uc, const float* up, const float* coefC,
                 const float* den, const float* coefQ, const Layout& L, const Weights<float>& W,
                 const TiledContext& ctx, cudaStream_t st) {
     auto kernel = stencil3d_vec4<R, VD, MINB, QS, ROT>;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     cudaGetDevice(&dev);
     const size_t smem = vec_smem_bytes<R, VD, QS>();
@@ -1111,7 +1112,7 @@ void launch_vec(float* un, const float* uc, const float* up, const float* coefC,
     const int ty = (int)((L.ny - 2 * R + 127) / 128);
     const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
     const int nzi = (int)(L.nz - 2 * R);
-    static int per_sm_of[64] = {};  // resident CTAs per SM, queried once per device
+    static std::atomic<int> per_sm_of[64];  // resident CTAs per SM, queried once per device
     if (!per_sm_of[dev & 63]) {
         int v = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, kThreads, smem);
@@ -1135,7 +1136,7 @@ void launch_vecp(float* un, const float* uc, const float* up, const float* coefC
                  const float* den, const float* coefQ, const Layout& L, const Weights<float>& W,
                  const TiledContext& ctx, cudaStream_t st) {
     auto kernel = stencil3d_vec4p<R, VD, MINB, GZ>;
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     cudaGetDevice(&dev);
     const size_t smem = vec_smem_bytes<R, VD, VD && !GZ>();
@@ -1146,7 +1147,7 @@ void launch_vecp(float* un, const float* uc, const float* up, const float* coefC
     const int ty = (int)((L.ny - 2 * R + 127) / 128);
     const int tx = (int)((L.nx - 2 * R + kWarps - 1) / kWarps);
     const int nzi = (int)(L.nz - 2 * R);
-    static int per_sm_of[64] = {};  // resident CTAs per SM, queried once per device
+    static std::atomic<int> per_sm_of[64];  // resident CTAs per SM, queried once per device
     if (!per_sm_of[dev & 63]) {
         int v = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, kThreads, smem);
