@@ -206,13 +206,22 @@ class SpaceModel:
             ramp = np.pad(np.zeros(self.shape, dtype=self.dtype),
                           pad_width=self.nbl_pad_width, mode="linear_ramp",
                           end_values=self.nbl_pad_width)
-            mask = (ramp ** self.damping_polynomial_degree) * self.damping_alpha
-            self._cache['damp'] = np.pad(mask, pad_width=self.halo_pad_width)
+            # in place, the same float32 operations; with degree >= 1 the
+            # zero core stays zero, so only the layer slabs are raised
+            deg = self.damping_polynomial_degree
+            views = _layer_slabs(ramp, self.nbl_pad_width) if deg >= 1 else [ramp]
+            for v in views:
+                np.power(v, deg, out=v)
+                v *= self.damping_alpha
+            self._cache['damp'] = np.pad(ramp, pad_width=self.halo_pad_width)
         return self._cache['damp']
 
     def _edge_padded(self, data):
-        data = np.pad(data, pad_width=self.nbl_pad_width, mode="edge")
-        return np.pad(data, pad_width=self.halo_pad_width, mode="edge")
+        # edge padding of an edge-padded array is one edge padding with the
+        # summed widths: the layer and the halo in a single copy
+        width = tuple((a + c, b + d) for (a, b), (c, d)
+                      in zip(self.nbl_pad_width, self.halo_pad_width))
+        return np.pad(data, pad_width=width, mode="edge")
 
     @property
     def extended_grid(self):
@@ -251,6 +260,24 @@ class SpaceModel:
         index = (slice(None),) + tuple(
             slice(nbl[2 * a], -nbl[2 * a + 1]) for a in range(self.dimension))
         return u[index]
+
+
+def _layer_slabs(a, widths):
+    """Views of ``a`` covering each point outside the core box (``widths``
+    per axis: before, after) exactly once: for each axis, the before and
+    after slabs over the core range of the axes before it."""
+    views = []
+    for axis in range(a.ndim):
+        index = [slice(widths[b][0], a.shape[b] - widths[b][1]) if b < axis else slice(None)
+                 for b in range(a.ndim)]
+        lo, hi = widths[axis]
+        if lo:
+            index[axis] = slice(0, lo)
+            views.append(a[tuple(index)])
+        if hi:
+            index[axis] = slice(a.shape[axis] - hi, a.shape[axis])
+            views.append(a[tuple(index)])
+    return views
 
 
 class TimeModel:
