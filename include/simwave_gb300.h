@@ -339,14 +339,15 @@ int simwave_batch_release(simwave_batch *batch, int shot_id);
 /* Tuning: stencil tile height (8, 16 or 32 rows) for one space order. */
 int simwave_batch_set_tile_rows(simwave_batch *batch, int space_order, int rows);
 /* Tuning: time-blocking depth for one space order -- 1 (default: a launch
- * per step), or 2..4 steps per launch where depth x space_order / 2 <= 32
- * (and the tile keeps >= 64 owned columns). A tile stages 96 rows of
- * u_cur and u_prev once and advances them `depth` steps in shared memory
- * (sources, boundary conditions and receiver records included), trading
- * recomputed tile margins for fewer passes over HBM. Shots with variable
- * density, a source window reaching into the halo, or a receiver window
- * wider than a tile keep depth 1; results equal depth 1's within float32
- * rounding (receiver sums are added per tile). */
+ * per step), or 2..4 steps per launch where depth x space_order / 2 <= 36
+ * (the tile keeps >= 32 owned rows) and the tile keeps >= 64 owned
+ * columns. A tile stages 104 rows of u_cur, u_prev, C and Q once and
+ * advances them `depth` steps in shared memory (sources, boundary
+ * conditions and receiver records included), trading recomputed tile
+ * margins for fewer passes over HBM. Shots with variable density or a
+ * source window reaching into the halo keep depth 1. Results equal depth
+ * 1's bit for bit (receiver windows are copied per tile and summed in the
+ * per-step order). */
 int simwave_batch_set_depth(simwave_batch *batch, int space_order, int depth);
 /* Depth a shot runs at under the current settings. */
 int simwave_batch_depth(simwave_batch *batch, int shot_id, int *depth);

@@ -98,7 +98,7 @@ __device__ __forceinline__ bool active(const Shot& s) { return s.n <= s.stop; }
 // DX on each side are recomputed margin. After step k of the block the
 // region's rows are exact k R rows further in and its computed columns
 // (k - 1) R columns further in, so after K steps the owned points are.
-constexpr int kTbRows = 96;
+constexpr int kTbRows = 104;
 
 struct TbGeom {
     int mz, oz, dx, ox;
@@ -1813,8 +1813,9 @@ extern "C" int simwave_batch_set_depth(simwave_batch* b, int space_order, int de
         if (!b || space_order < 2 || space_order > 20 || space_order % 2 || depth < 1 ||
             depth > 4 || (depth > 1 && !sw::batch::tb_supported(space_order / 2, depth)))
             sw::batch::fail(SIMWAVE_E_ARGUMENT,
-                            "space_order even in 2..20; depth 1, or 2..4 with (depth x "
-                            "space_order / 2) <= 32 and the tile's owned width >= 64");
+                            "space_order even in 2..20; depth 1, or 2..4 with the tile "
+                            "keeping >= 32 owned rows (depth x space_order / 2 <= 36) and "
+                            ">= 64 owned columns");
         std::lock_guard<std::mutex> lock(sw::batch::g_mutex);
         Engine* e = sw::batch::engine(b);
         e->depth[space_order / 2] = depth;
