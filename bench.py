@@ -20,7 +20,7 @@ Gpts/s, whole job over all ranks.
   roofline    stencil kernel: algorithmic bytes per launch (20 B per interior
               point: read u_cur, u_prev, velocity, density, write u_next) over
               its mean launch time (CUDA events on the same stream)
-  cpu_baseline the CPU checker (C restatement, OpenMP, all host cores) on a
+  cpu_baseline the CPU oracle (C restatement, OpenMP, all host cores) on a
               bounded sample of the same workload (fewer time steps)
 
 Extra legs in the same line (rank 0): `batched` (96 2D shots advanced
@@ -393,13 +393,13 @@ def config1_arguments(dtype=np.float32):
 def config1_leg(reps=20):
     """Config 1 (L2- and launch-bound): Gpts/s of plain device calls, of the
     same shot through the graph-captured batch engine, of the drop-in with
-    host buffers, and of the CPU checker on the full run (with the relative
+    host buffers, and of the CPU oracle on the full run (with the relative
     L2 difference of the shot record against it)."""
     import contextlib
     import io
     import torch
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the CPU baseline and checker of this leg
+    import oracle  # the CPU baseline and oracle of this leg
     from simwave_gb300.backend.middleware import Middleware
     from simwave_gb300.batch import BatchEngine
     from simwave_gb300.device import DeviceProblem
@@ -469,7 +469,7 @@ def accuracy_leg():
     the shot record and the final wavefield. Config 2 runs its first 51 of
     1201 steps; configs 3-5 use representative shots."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the checker of this leg
+    import oracle  # the oracle of this leg
     from simwave_gb300.device import DeviceProblem
 
     def rel(a, b):
@@ -692,7 +692,7 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU checker timing (bounded sample)
+# CPU oracle timing (bounded sample)
 
 def cpu_sample(steps, threads=None, n=384):
     """Gpts/s of the C restatement on `steps` time steps of the workload."""

@@ -1,4 +1,4 @@
-"""ctypes front for the CPU checker (TEST INFRASTRUCTURE ONLY).
+"""ctypes front for the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
 this module; the product package never imports it.

@@ -1,7 +1,7 @@
 /*
  * wave_oracle.c -- CPU restatement of simwave's forward time loop.
  *
- * TEST INFRASTRUCTURE ONLY: this file is the checker for the GPU library.
+ * TEST INFRASTRUCTURE ONLY: this file is the oracle for the GPU library.
  * It is built into oracle/_build/liboracle.so and is loaded only by tests/,
  * by __graft_entry__.smoke() and by bench.py's CPU-baseline leg. The product
  * (simwave_gb300) never links or calls it.

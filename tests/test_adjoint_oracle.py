@@ -1,4 +1,4 @@
-"""The float64 adjoint-state gradient used as the checker of the GPU
+"""The float64 adjoint-state gradient used as the oracle of the GPU
 gradient: its forward is the C restatement's forward, and its gradient is
 the derivative of that forward (central finite differences in float64),
 for every boundary-condition mix, with waves that reach every edge."""

@@ -1,4 +1,4 @@
-"""The batch engine against the CPU checker and the single-shot entry: mixed
+"""The batch engine against the CPU oracle and the single-shot entry: mixed
 orders, densities, grid sizes, boundary sets and saving strides advanced
 together give each shot's own result."""
 import numpy as np
@@ -28,7 +28,7 @@ def _shots(seed=0, count=7):
     return kws
 
 
-def test_batch_matches_checker():
+def test_batch_matches_oracle():
     from simwave_gb300.batch import run_batch
     from simwave_gb300.device import DeviceProblem
     kws = _shots(seed=3)
@@ -114,8 +114,8 @@ def _cd_shots(seed, count):
 
 
 @pytest.mark.parametrize("depth", [2, 3, 4])
-def test_time_blocked_batch_matches_checker(depth):
-    """Each time-blocked shot against the checker and the per-step batch,
+def test_time_blocked_batch_matches_oracle(depth):
+    """Each time-blocked shot against the oracle and the per-step batch,
     advanced in chunks that end inside time blocks."""
     from simwave_gb300.batch import BatchEngine
     from simwave_gb300.device import DeviceProblem
@@ -155,7 +155,7 @@ def test_time_blocked_batch_matches_checker(depth):
 
 def test_time_blocking_skips_what_it_cannot_run():
     """Variable density and source windows reaching into the halo keep the
-    per-step kernels (and still match the checker)."""
+    per-step kernels (and still match the oracle)."""
     from simwave_gb300.batch import BatchEngine
     from simwave_gb300.device import DeviceProblem
     vd = random_problem(sw, 2, 4, True, "null_neumann", 0, shape=(120, 140), tf=0.05, seed=1)

@@ -1,4 +1,4 @@
-"""Edge cases of the forward operator against the CPU checker: no receivers,
+"""Edge cases of the forward operator against the CPU oracle: no receivers,
 an all-zero wavelet, a run resumed across two calls, source and receiver
 windows that reach into the halo, and the largest radius on the smallest
 grid the operator accepts (one interior point per axis)."""

@@ -1,4 +1,4 @@
-"""GPU parity: the sm_103a library against the CPU checker.
+"""GPU parity: the sm_103a library against the CPU oracle.
 
 Tolerances (relative L2 over the whole output array):
   float32: 1e-4 (the contract stated for this path), float64: 1e-9.
@@ -51,7 +51,7 @@ def test_fixture_parity(name):
     u, rec = gpu_forward(kw)
     if name == "3d_vd_so6_noncube_s0_f32":
         # nx != ny: the reference's x first-derivative stride differs from the
-        # layout's; compare with the checker on the layout stride instead
+        # layout's; compare with the oracle on the layout stride instead
         expected_u, expected_rec = port_forward(kw, x_stride="layout")
     if isinstance(expected_u, tuple):
         slot, expected_u = expected_u
@@ -170,7 +170,7 @@ POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3,
 @pytest.mark.parametrize("vd", [False, True])
 def test_tiled_and_generic_kernels_agree(order, vd, policy):
     """Each tiled 3D kernel variant against the one-thread-per-point kernel
-    and the checker, on shapes that leave partial tiles in x and y."""
+    and the oracle, on shapes that leave partial tiles in x and y."""
     from simwave_gb300.backend import _lib
     from simwave_gb300.device import DeviceProblem
     bc = ("null_neumann", "null_dirichlet", "none", "null_neumann",
@@ -203,7 +203,7 @@ def test_tiled_and_generic_kernels_agree(order, vd, policy):
 @pytest.mark.parametrize("vd", [False, True])
 def test_tiled2d_and_generic_kernels_agree(order, vd):
     """The tiled 2D kernel against the one-thread-per-point kernel and the
-    checker (partial tiles in both axes)."""
+    oracle (partial tiles in both axes)."""
     from simwave_gb300.device import DeviceProblem
     bc = ("null_neumann", "null_dirichlet", "null_dirichlet", "null_neumann")
     kw = random_problem(sw, 2, order, vd, bc, 3, shape=(77, 301), tf=0.04,
@@ -235,7 +235,7 @@ def test_tiled2d_and_generic_kernels_agree(order, vd):
 @pytest.mark.parametrize("order,vd", [(2, False), (4, True), (8, False), (12, True)])
 def test_fused_step_sources_across_tiles(order, vd):
     """One launch per step with many wide source windows that straddle tile
-    borders and the damping layer, against the checker."""
+    borders and the damping layer, against the oracle."""
     from simwave_gb300.device import DeviceProblem
     bc = ("null_dirichlet", "null_neumann", "null_neumann", "null_dirichlet")
     kw = random_problem(sw, 2, order, vd, bc, 0, shape=(126, 290), tf=0.05, seed=order,

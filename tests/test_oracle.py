@@ -1,4 +1,4 @@
-"""The CPU checker is pinned to the reference: bit-identical to the outputs
+"""The CPU oracle is pinned to the reference: bit-identical to the outputs
 the reference's own C path produced for every golden fixture, and (where the
 reference tree was compiled into oracle/_ref) to the reference kernels on
 fresh cases."""
