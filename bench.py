@@ -64,7 +64,7 @@ def _smooth_noise(shape, sigma, seed):
     return g / np.abs(g).max()
 
 
-def config2_model(n=384):
+def vd3d_model(n=384):
     if n in _MODEL_CACHE:
         return _MODEL_CACHE[n]
     z = np.linspace(0.0, 1.0, n, dtype=np.float32)
@@ -78,13 +78,13 @@ def config2_model(n=384):
     return vel, den
 
 
-def config2_arguments(timesteps=None, n=384, stride=50, dtype=np.float32):
+def vd3d_arguments(timesteps=None, n=384, stride=50, dtype=np.float32):
     """Middleware keyword arguments of the 3D benchmark shot.
 
     ``timesteps`` truncates the run (same dt and wavelet samples) for tests
     and bounded CPU samples."""
     import simwave_gb300 as sw
-    vel, den = config2_model(n)
+    vel, den = vd3d_model(n)
     h = 12.5
     top = (n - 1) * h
     sm = sw.SpaceModel((0, top, 0, top, 0, top), (h, h, h), vel, den,
@@ -129,7 +129,7 @@ def smooth_velocity(shape, rng, lo=1500.0, hi=4500.0, modes=6):
     return (lo + (hi - lo) * f).astype(np.float32)
 
 
-def config3_arguments(nshots=96, seed=7, max_side=2048, dtype=np.float32, pick=None):
+def batch2d_arguments(nshots=96, seed=7, max_side=2048, dtype=np.float32, pick=None):
     """The batched workload: 2D constant-density shots with seeded grids of
     256..max_side points per side (10 m), orders {4, 8, 12, 16, 20}, smooth
     random velocity 1500-4500 m/s, 50-point damping layer, an 8-25 Hz Ricker
@@ -170,7 +170,7 @@ def batched_leg(nshots=96, max_side=2048):
     import torch
     from simwave_gb300.batch import BatchEngine, autotune, run_batch
     from simwave_gb300.device import DeviceProblem
-    kws = config3_arguments(nshots, max_side=max_side)
+    kws = batch2d_arguments(nshots, max_side=max_side)
     probs = [DeviceProblem(k) for k in kws]
     updates = sum(interior_updates(k)[1] for k in kws)
     stream = torch.cuda.current_stream()
@@ -238,7 +238,7 @@ def batched_leg(nshots=96, max_side=2048):
                       "included); drop-in: wall clock of the host calls, copies included"}
 
 
-def config4_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320,
+def served_requests(nreq=40, seed=11, rate=200.0, frac3d=0.25, max2d=2048, max3d=320,
                      dtype=np.float32, pick=None):
     """The served workload: Poisson arrivals (seeded, ``rate`` per second) of
     2D shots (512..max2d per side) and 3D shots (128..max3d per side), orders
@@ -321,7 +321,7 @@ def served_leg(nreq=40):
     import torch
     from simwave_gb300.backend.middleware import Middleware
     from simwave_gb300.serve import Request, ShotServer, latency_summary
-    reqs = config4_requests(nreq)
+    reqs = served_requests(nreq)
     arrivals = [r.arrival for r in reqs]
     updates = sum(interior_updates(r.kwargs)[1] for r in reqs)
     # load every kernel class of the workload on both paths first
@@ -370,7 +370,7 @@ def served_leg(nreq=40):
             "speedup_shots_per_s": round(served["shots_per_s"] / seq["shots_per_s"], 2)}
 
 
-def config1_arguments(dtype=np.float32):
+def readme2d_arguments(dtype=np.float32):
     """The reference README's 2D case: 512^2 model (1500 m/s above row 100,
     2000 below) interpolated onto the 513^2 grid of a 5120 m box at 10 m,
     order 4, no damping layer, boundaries (null_neumann, null_dirichlet,
@@ -390,8 +390,9 @@ def config1_arguments(dtype=np.float32):
     return sw.Solver(sm, tm, src, rec, sw.RickerWavelet(10.0, tm)).forward_arguments()
 
 
-def config1_leg(reps=20):
-    """Config 1 (L2- and launch-bound): Gpts/s of plain device calls, of the
+def plain2d_leg(reps=20):
+    """The reference README's 2D shot (513² grid, order 4; L2- and
+    launch-bound): Gpts/s of plain device calls, of the
     same shot through the graph-captured batch engine, of the drop-in with
     host buffers, and of the CPU oracle on the full run (with the relative
     L2 difference of the shot record against it)."""
@@ -403,7 +404,7 @@ def config1_leg(reps=20):
     from simwave_gb300.backend.middleware import Middleware
     from simwave_gb300.batch import BatchEngine
     from simwave_gb300.device import DeviceProblem
-    kw = config1_arguments()
+    kw = readme2d_arguments()
     pts, updates = interior_updates(kw)
     dp = DeviceProblem(kw)
 
@@ -462,12 +463,13 @@ def config1_leg(reps=20):
 
 
 def accuracy_leg():
-    """Per configuration: the float32 error of the GPU and of the reference's
+    """Per workload: the float32 error of the GPU and of the reference's
     C path (the CPU port, bit-identical to the reference build) against the
     float64 run (the CPU port in float64 on the same model, built in float64
     by the front end as the reference's front end does), relative L2 over
-    the shot record and the final wavefield. Config 2 runs its first 51 of
-    1201 steps; configs 3-5 use representative shots."""
+    the shot record and the final wavefield. The 472³ 3D shot runs its
+    first 51 of 1201 steps; the batched, served and inversion workloads use
+    representative shots."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the oracle of this leg
     from simwave_gb300.device import DeviceProblem
@@ -489,17 +491,17 @@ def accuracy_leg():
         dp.status()
         return dp.u_full_numpy(), dp.shot_record_numpy()
 
-    true, smooth = config5_models()
-    _, dt5 = config5_arguments(true, nshots=1)
+    true, smooth = inversion_models()
+    _, dt5 = inversion_arguments(true, nshots=1)
     cases = [
-        ("1 plain 2D, 513^2 so4", lambda d: config1_arguments(dtype=d)),
-        ("2 3D VD so8 472^3, steps 1-51", lambda d: config2_arguments(timesteps=51, dtype=d)),
-        ("3 batched shot 3 (1665x1127 so4)", lambda d: config3_arguments(12, pick={3}, dtype=d)[0]),
-        ("3 batched shot 7 (666x1382 so16)", lambda d: config3_arguments(12, pick={7}, dtype=d)[0]),
-        ("4 served 2D Gardner (1330x811 so12)", lambda d: config4_requests(40, pick={0}, dtype=d)[0].kwargs),
-        ("4 served 3D VD (204^3 so8)", lambda d: config4_requests(40, pick={11}, dtype=d)[0].kwargs),
-        ("5 inversion shot 0 forward (459x1809 so8)",
-         lambda d: config5_arguments(smooth, dt=dt5, nshots=1, dtype=d)[0][0]),
+        ("plain 2D, 513^2 so4", lambda d: readme2d_arguments(dtype=d)),
+        ("3D VD so8 472^3, steps 1-51", lambda d: vd3d_arguments(timesteps=51, dtype=d)),
+        ("batched shot 3 (1665x1127 so4)", lambda d: batch2d_arguments(12, pick={3}, dtype=d)[0]),
+        ("batched shot 7 (666x1382 so16)", lambda d: batch2d_arguments(12, pick={7}, dtype=d)[0]),
+        ("served 2D Gardner (1330x811 so12)", lambda d: served_requests(40, pick={0}, dtype=d)[0].kwargs),
+        ("served 3D VD (204^3 so8)", lambda d: served_requests(40, pick={11}, dtype=d)[0].kwargs),
+        ("inversion shot 0 forward (459x1809 so8)",
+         lambda d: inversion_arguments(smooth, dt=dt5, nshots=1, dtype=d)[0][0]),
     ]
     rows = []
     for name, build in cases:
@@ -507,7 +509,7 @@ def accuracy_leg():
         u64, r64 = cpu(kw64)
         u32, r32 = cpu(kw32)
         gu, gr = gpu(kw32)
-        rows.append({"config": name,
+        rows.append({"workload": name,
                      "gpu_f32_vs_f64": {"shot_record": rel(gr, r64), "wavefield": rel(gu, u64)},
                      "ref_f32_vs_f64": {"shot_record": rel(r32, r64), "wavefield": rel(u32, u64)},
                      "gpu_vs_ref_f32": {"shot_record": rel(gr, r32), "wavefield": rel(gu, u32)}})
@@ -515,7 +517,7 @@ def accuracy_leg():
     return rows
 
 
-def config5_models(seed=5):
+def inversion_models(seed=5):
     """The inversion workload's models on a (351, 1701) grid of 10 m (nz = 351,
     nx = 1701): 12 layers from 1500 to 5500 m/s cut by two dipping faults
     (seeded), and its Gaussian smoothing with sigma = 20 points (the model
@@ -539,7 +541,7 @@ def config5_models(seed=5):
     return true, smooth
 
 
-def config5_arguments(vel, dt=None, nshots=16, damping_points=50, dtype=np.float32):
+def inversion_arguments(vel, dt=None, nshots=16, damping_points=50, dtype=np.float32):
     """Middleware keyword arguments of the inversion shots on ``vel``: so 8,
     8 Hz Ricker, tf 3.0 s, sources at 20 m depth spread over x, 1701
     receivers at 10 m depth (one per grid column), a 50-point damping layer
@@ -572,9 +574,9 @@ def gradient_leg(nshots=16, steps=1, interval=None, workers=4):
     import torch
     from simwave_gb300.device import DeviceProblem
     from simwave_gb300.gradient import default_interval, misfit_gradient, shot_record
-    true, smooth = config5_models()
-    kw_true, dt = config5_arguments(true, nshots=nshots)
-    kw_model, _ = config5_arguments(smooth, dt=dt, nshots=nshots)
+    true, smooth = inversion_models()
+    kw_true, dt = inversion_arguments(true, nshots=nshots)
+    kw_model, _ = inversion_arguments(smooth, dt=dt, nshots=nshots)
     observed = []
     for kw in kw_true:
         p = DeviceProblem(kw)
@@ -700,7 +702,7 @@ def cpu_sample(steps, threads=None, n=384):
     import oracle
     threads = threads or os.cpu_count()
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    kw = config2_arguments(timesteps=steps, stride=0, n=n)
+    kw = vd3d_arguments(timesteps=steps, stride=0, n=n)
     pts, updates = interior_updates(kw)
     _, _, secs = oracle.forward("port", x_stride="layout", **kw)
     return updates / secs / 1e9, secs, threads
@@ -838,7 +840,7 @@ def main():
     from simwave_gb300.device import DeviceProblem
 
     torch.cuda.set_device(local)
-    kw = config2_arguments(timesteps=args.timesteps, n=args.n)
+    kw = vd3d_arguments(timesteps=args.timesteps, n=args.n)
     pts, updates = interior_updates(kw)
     dp = DeviceProblem(kw, device="cuda:%d" % local)
     stream = torch.cuda.current_stream()
@@ -931,7 +933,7 @@ def main():
 
     batched = served = gradient = plain2d = None
     if rank == 0:
-        plain2d = leg(config1_leg)
+        plain2d = leg(plain2d_leg)
     if rank == 0 and not args.no_batched:
         batched = leg(batched_leg)
     if rank == 0 and not args.no_served:

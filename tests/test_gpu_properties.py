@@ -103,7 +103,7 @@ def test_solution_2d_golden(order):
 @pytest.fixture(scope="module")
 def big_problem():
     import bench
-    return bench.config2_arguments(timesteps=61, stride=4)
+    return bench.vd3d_arguments(timesteps=61, stride=4)
 
 
 def test_full_size_source_linearity(big_problem):
@@ -163,7 +163,7 @@ def test_full_size_stride_invariance(big_problem):
     assert torch.equal(dp4.receivers, rec0)
 
 
-def test_config1_float32_error_matches_reference():
+def test_readme2d_float32_error_matches_reference():
     """The reference README's 2D case (513^2, order 4, T 328, both boundary
     phases): the GPU's float32 error against the float64 run is the
     reference float32 path's own error to within a factor of two."""
@@ -177,7 +177,7 @@ def test_config1_float32_error_matches_reference():
         u, r, _ = oracle.forward("port", **k)
         return u, r
 
-    kw32, kw64 = bench.config1_arguments(np.float32), bench.config1_arguments(np.float64)
+    kw32, kw64 = bench.readme2d_arguments(np.float32), bench.readme2d_arguments(np.float64)
     u64, r64 = cpu(kw64)
     u32, r32 = cpu(kw32)
     dp = DeviceProblem(kw32)
