@@ -290,19 +290,21 @@ int simwave_device_status(void *stream);
  * simwave_forward_device on caller-owned device arrays, but allocates no
  * device memory at all: no cudaMalloc, cudaFree or allocating library call.
  * It exists for callers that cannot let us allocate while they run: a host
- * framework that owns the device memory budget through its own pool, a
+ * framework that owns the device memory budget through its own pool, or a
  * serving loop in which an allocation would synchronise the device and stall
- * unrelated work, or code that enqueues work while a stream is captured.
- * Its scratch (two per-point coefficient grids and 256 bytes of status
- * words) lives in one file-scope device array of
+ * unrelated work. Its scratch (two per-point coefficient grids and 256 bytes
+ * of status words) lives in one file-scope device array of
  * SIMWAVE_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
  * until the process exits. Limits: 3D float32 problems only; a grid of at
  * most (SIMWAVE_NOALLOC_SCRATCH_BYTES - 256) / 8 pitched points (larger grids
  * are refused with SIMWAVE_E_ARGUMENT and a simwave_last_error() message);
- * no SIMWAVE_FLAG_TIME_KERNELS; the layout must suit the tiled kernel (the
- * one simwave_layout() returns does). The first call on a device looks up
- * the array's device address (with that device current); make it before any
- * stream capture. The call waits for `stream` before returning. All calls
+ * of the flags only SIMWAVE_FLAG_WINDOWS_CHECKED (any other flag is
+ * refused); the layout must suit the tiled kernel (the one simwave_layout()
+ * returns does). The call reads results back to the host and waits for
+ * `stream` mid-call, so it must not be made on a stream that is being
+ * captured into a CUDA graph: such a stream is refused with
+ * SIMWAVE_E_ARGUMENT before any work is enqueued. The first call on a device
+ * looks up the array's device address (with that device current). All calls
  * share the one array and its status words are reset at the start of each
  * call: calls that overlap on the GPU race on it and must be serialised.
  * No reference counterpart. */
@@ -366,6 +368,9 @@ typedef struct simwave_stats {
                                  in one persistent launch, 3 tiled 2D, each
                                  step (stencil, sources, boundaries,
                                  receivers) in one launch */
+    int stencil_kernel;       /* 3D float32 tiled runs: the SIMWAVE_POLICY_*
+                                 of the stencil kernel launched (AUTO
+                                 resolved); 0 otherwise */
 } simwave_stats;
 
 /* No reference counterpart (the reference returns only its wall time). */

@@ -56,7 +56,8 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_size_t),
                 ("h2d_bytes", ctypes.c_size_t),
                 ("d2h_bytes", ctypes.c_size_t),
-                ("stencil_variant", ctypes.c_int)]
+                ("stencil_variant", ctypes.c_int),
+                ("stencil_kernel", ctypes.c_int)]
 
 
 def last_stats():

@@ -244,7 +244,7 @@ struct Run {
 template <typename T, int DIM, bool VD>
 static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
                            const T* uc, const T* up, cudaStream_t st,
-                           int* variant) {
+                           int* variant, int* kernel) {
     const Layout& L = R.L;
     const T dt2 = R.dt * R.dt;
     if constexpr (std::is_same<T, float>::value && DIM == 2) {
@@ -258,8 +258,8 @@ static void launch_stencil(const Run<T>& R, const TiledContext& tctx, T* un,
     }
     if constexpr (std::is_same<T, float>::value && DIM == 3) {
         if (tctx.ok) {
-            tiled_launch(tctx, VD, un, uc, up, tctx.coefC, R.den, tctx.coefQ, L,
-                         R.W, R.dt, dt2, st);
+            *kernel = tiled_launch(tctx, VD, un, uc, up, tctx.coefC, R.den, tctx.coefQ, L,
+                                   R.W, R.dt, dt2, st);
             *variant = 1;
             SW_LAUNCHED("stencil3d_tiled");
             return;
@@ -433,7 +433,8 @@ static void run_steps(const Run<T>& R, const Schedule& S, cudaStream_t st,
             }
         }
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i], st));
-        launch_stencil<T, DIM, VD>(R, tctx, un, uc, up, st, &stats.stencil_variant);
+        launch_stencil<T, DIM, VD>(R, tctx, un, uc, up, st, &stats.stencil_variant,
+                                   &stats.stencil_kernel);
         if (ev) SW_CUDA(cudaEventRecord((*ev)[2 * i + 1], st));
         stats.stencil_launches++;
         stats.kernel_launches++;

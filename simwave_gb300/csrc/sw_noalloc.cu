@@ -3,10 +3,9 @@
 //
 // Who needs it: callers that must not (or cannot) allocate device memory
 // while they run us -- a host framework that owns the whole device memory
-// budget through its own pool and forbids allocations behind its back, a
+// budget through its own pool and forbids allocations behind its back, or a
 // latency-critical serving loop where cudaMalloc/cudaFree would synchronise
-// the device and stall other work, or code that enqueues work while a stream
-// is being captured into a CUDA graph. The regular device entry keeps its
+// the device and stall other work. The regular device entry keeps its
 // scratch (per-point coefficient grids, a few status words) in buffers it
 // allocates on first use; this entry keeps the same scratch in one
 // file-scope device array of fixed size instead.
@@ -21,12 +20,17 @@
 //     kernel (pitch a multiple of 4 elements, lead + r a multiple of 32,
 //     16-byte aligned arrays: what simwave_layout() returns), otherwise the
 //     call is refused;
-//   * SIMWAVE_FLAG_TIME_KERNELS is refused (it needs event objects);
+//   * flags: only SIMWAVE_FLAG_WINDOWS_CHECKED is honoured; every other flag
+//     (timing events, the generic kernel, per-step launches) is refused;
+//   * the call must not be made on a stream that is being captured into a
+//     CUDA graph: it reads the zero-box bounds and the status word back to
+//     the host and waits for its stream mid-call, which capture forbids, so
+//     a capturing stream is refused up front (the capture stays intact);
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (that device current); make that first call
-//     before any stream capture;
-//   * the call waits for its stream before returning (it reads the zero-box
-//     bounds back mid-run and the status word at the end);
+//     cudaGetSymbolAddress (that device current);
+//   * the stencil reads the density's z derivative from a shared-memory
+//     queue (the regular entry may form it once per run in an allocated
+//     grid instead): same operator, another kernel variant;
 //   * every call shares the one array: the status words are cleared at the
 //     start of each call, and calls that overlap on the GPU (from several
 //     host threads or streams at once) race on it -- serialise them.
@@ -167,6 +171,17 @@ static int run(const simwave_problem* P, cudaStream_t st) {
         refuse(SIMWAVE_E_ARGUMENT, "the allocation-free entry runs 3D float32 problems only");
     if (P->flags & SIMWAVE_FLAG_TIME_KERNELS)
         refuse(SIMWAVE_E_ARGUMENT, "SIMWAVE_FLAG_TIME_KERNELS is not available without allocation");
+    if (P->flags & ~SIMWAVE_FLAG_WINDOWS_CHECKED)
+        refuse(SIMWAVE_E_ARGUMENT,
+               "the allocation-free entry honours only SIMWAVE_FLAG_WINDOWS_CHECKED");
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        NA_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            refuse(SIMWAVE_E_ARGUMENT,
+                   "the allocation-free entry waits for its stream mid-call and cannot run "
+                   "on a stream that is being captured");
+    }
     if (P->space_order < 2 || P->space_order > 20 || P->space_order % 2)
         refuse(SIMWAVE_E_ARGUMENT, "space_order must be even in 2..20");
     const int r = P->space_order / 2;
@@ -181,14 +196,17 @@ static int run(const simwave_problem* P, cudaStream_t st) {
     for (int e = 0; e < 6; e++)
         if (P->boundary_conditions[e] > 2)
             refuse(SIMWAVE_E_ARGUMENT, "boundary code must be 0, 1 or 2");
-    const size_t grid = P->nz * P->nx * P->pitch;  // elements of one pitched grid
+    // elements of one pitched grid, each product checked before it is formed
+    const size_t capacity = (kScratchBytes - kWordsBytes) / (2 * sizeof(float));
+    if (P->pitch > capacity || P->nx > capacity / P->pitch ||
+        P->nz > capacity / (P->nx * P->pitch))
+        refuse(SIMWAVE_E_ARGUMENT,
+               "grid of " + std::to_string(P->nz) + " x " + std::to_string(P->nx) + " x " +
+                   std::to_string(P->pitch) + " pitched points exceeds the " +
+                   "allocation-free scratch (" + std::to_string(capacity) + " points)");
+    const size_t grid = P->nz * P->nx * P->pitch;
     if (P->num_snapshots > 1 && P->slot_stride < grid)
         refuse(SIMWAVE_E_ARGUMENT, "slot_stride smaller than one grid");
-    const size_t capacity = (kScratchBytes - kWordsBytes) / (2 * sizeof(float));
-    if (grid > capacity)
-        refuse(SIMWAVE_E_ARGUMENT,
-               "grid of " + std::to_string(grid) + " pitched points exceeds the " +
-                   "allocation-free scratch (" + std::to_string(capacity) + " points)");
     if (P->begin_timestep < 1) refuse(SIMWAVE_E_ARGUMENT, "begin_timestep must be >= 1");
     if (P->num_sources && P->end_timestep >= P->begin_timestep) {
         const size_t need = P->wavelet_count > 1 ? P->end_timestep * P->num_sources

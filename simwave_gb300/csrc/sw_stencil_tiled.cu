@@ -1290,7 +1290,7 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
     return true;
 }
 
-void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, const float* up,
+int tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, const float* up,
                   const float* vel, const float* den, const float* damp, const Layout& L,
                   const Weights<float>& W, float dt, float dt2, cudaStream_t st) {
     const int policy = kernel_policy();
@@ -1311,7 +1311,7 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, 
             if (one) launch_vecp_any<RR, false, 1>(un, uc, up, vel, den, damp, L, W, ctx, st); \
             else launch_vecp_any<RR, false, 2>(un, uc, up, vel, den, damp, L, W, ctx, st);     \
         }                                                                                     \
-        return;
+        return high;
         switch (L.r) { SW_VECH(5) SW_VECH(6) SW_VECH(7) SW_VECH(8) }
 #undef SW_VECH
     }
@@ -1323,7 +1323,7 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, 
     case RR:                                                                                    \
         if (vd) launch_vec_policy<RR, true>(policy, un, uc, up, vel, den, damp, L, W, ctx, st); \
         else launch_vec_policy<RR, false>(policy, un, uc, up, vel, den, damp, L, W, ctx, st);   \
-        return;
+        return policy == SIMWAVE_POLICY_AUTO ? auto_policy(RR, vd) : policy;
         switch (L.r) { SW_VEC(1) SW_VEC(2) SW_VEC(3) SW_VEC(4) }
 #undef SW_VEC
     }
@@ -1338,6 +1338,7 @@ void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, 
         default: break;
     }
 #undef SW_CASE
+    return SIMWAVE_POLICY_SCALAR_TILED;
 }
 
 }  // namespace sw

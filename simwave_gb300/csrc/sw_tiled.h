@@ -31,7 +31,8 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
                    long long nslots, long long slot_stride, const float* den);
 
 // `coefC` and `coefQ` are the per-point coefficients of form_coefficients.
-void tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc,
+// Returns the SIMWAVE_POLICY_* of the kernel launched.
+int tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc,
                   const float* up, const float* coefC, const float* den,
                   const float* coefQ, const Layout& L, const Weights<float>& W,
                   float dt, float dt2, cudaStream_t st);

@@ -191,11 +191,18 @@ def solution_case(sw, order):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = (sys.argv[1] if len(sys.argv) > 1 else
+                os.environ.get("SIMWAVE_REFERENCE_ROOT") or
+                os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))),
+                             "reference"))
+    if not os.path.isdir(os.path.join(ref_root, "simwave")):
+        sys.exit("reference checkout not found: pass its path (or set "
+                 "SIMWAVE_REFERENCE_ROOT)")
     install_shims()
     sys.path.insert(0, ref_root)
     import simwave as sw  # the reference package
-    manifest = {"reference_root": ref_root, "cases": {}}
+    manifest = {"reference_root": os.path.basename(os.path.abspath(ref_root)),
+                "cases": {}}
     workdir = tempfile.mkdtemp(prefix="simwave_golden_")
     cwd = os.getcwd()
     os.chdir(workdir)  # the reference Compiler writes ./tmp/<sha1>.so
