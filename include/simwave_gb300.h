@@ -265,6 +265,13 @@ int simwave_forward_device(const simwave_problem *problem, void *stream);
                                            arithmetic, density z-queue in shared
                                            memory, 2 CTAs per SM */
 #define SIMWAVE_POLICY_VEC_PACKED_1CTA 8 /* same, 1 CTA per SM */
+#define SIMWAVE_POLICY_TMEM 9           /* orders <= 8: packed arithmetic, the
+                                           u and density z queues in tensor
+                                           memory, damping from per-axis
+                                           tables; 8 x rows per CTA, 2 CTAs
+                                           per SM */
+#define SIMWAVE_POLICY_TMEM_WIDE 10     /* same, 16 x rows per CTA, 1 CTA per
+                                           SM */
 int simwave_set_kernel_policy(int policy);
 
 /* How the host-pointer entries move grids (process-wide).

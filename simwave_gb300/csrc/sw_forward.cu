@@ -314,14 +314,19 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         ctx.ok = false;
         const size_t n = (size_t)(L.dim == 3 ? L.nz * L.plane : L.nz * L.pitch);
         const bool gz = L.dim == 3 && wants_density_z(L, R.vd);
+        // tensor-memory kernel: per-axis tables of the damping mask
+        const bool tm = L.dim == 3 && ctx.tm;
+        const size_t ntab = tm ? (size_t)(L.nz + L.nx + L.ny + 32) : 0;
         void* scratch = nullptr;
-        SW_CUDA(cudaMallocAsync(&scratch, (gz ? 3 : 2) * n * sizeof(float) + 16 * sizeof(int),
+        SW_CUDA(cudaMallocAsync(&scratch,
+                                ((gz ? 3 : 2) * n + ntab) * sizeof(float) + 16 * sizeof(int),
                                 st));
         ctx.scratch = scratch;
         float* C = static_cast<float*>(scratch);
         float* Q = C + n;
         float* G = gz ? Q + n : nullptr;
-        int* words = reinterpret_cast<int*>(Q + (gz ? 2 : 1) * n);
+        float* tabs = Q + (gz ? 2 : 1) * n;
+        int* words = reinterpret_cast<int*>(tabs + ntab);
         form_coefficients(R.vel, R.damp, C, Q, (long long)n, (float)R.dt, st);
         SW_LAUNCHED("form_coefficients");
         if (G) {
@@ -331,12 +336,25 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         }
         find_zero_box(Q, L, words, st);
         SW_LAUNCHED("find_zero_box");
-        int box[7];
+        if (tm) {
+            damp_face_tables(R.damp, L, words, tabs, tabs + L.nz, tabs + L.nz + L.nx, words + 8,
+                             st);
+            SW_LAUNCHED("damp_face_tables");
+        }
+        int box[9];
         SW_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
         SW_CUDA(cudaStreamSynchronize(st));
         bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
         if (L.dim == 3) good = good && box[5] > box[4];
         for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
+        if (tm) {
+            ctx.damp = R.damp;
+            ctx.damp_tz = tabs;
+            ctx.damp_tx = tabs + L.nz;
+            ctx.damp_ty = tabs + L.nz + L.nx;
+            ctx.damp_faces_ok = good && box[8] == 0;
+            ctx.inv_dt = (float)(1.0 / (double)R.dt);
+        }
         ctx.coefC = C;
         ctx.coefQ = Q;
         ctx.err = device_words() + 7;
@@ -1198,7 +1216,7 @@ extern "C" int simwave_device_status(void* stream) {
 }
 
 extern "C" int simwave_set_kernel_policy(int policy) {
-    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_VEC_PACKED_1CTA)
+    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_TMEM_WIDE)
         return SIMWAVE_E_ARGUMENT;
     sw::set_kernel_policy(policy);
     return SIMWAVE_OK;

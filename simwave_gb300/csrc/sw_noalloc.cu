@@ -28,9 +28,10 @@
 //     a capturing stream is refused up front (the capture stays intact);
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (that device current);
-//   * the stencil reads the density's z derivative from a shared-memory
-//     queue (the regular entry may form it once per run in an allocated
-//     grid instead): same operator, another kernel variant;
+//   * the stencil is the one the regular entry runs, except where that one
+//     would read the density's z derivative from a grid formed once per run
+//     (it cannot be held in this scratch): the packed kernel then takes it
+//     from its shared-memory queue instead -- same operator;
 //   * every call shares the one array: the status words are cleared at the
 //     start of each call, and calls that overlap on the GPU (from several
 //     host threads or streams at once) race on it -- serialise them.
@@ -196,8 +197,13 @@ static int run(const simwave_problem* P, cudaStream_t st) {
     for (int e = 0; e < 6; e++)
         if (P->boundary_conditions[e] > 2)
             refuse(SIMWAVE_E_ARGUMENT, "boundary code must be 0, 1 or 2");
-    // elements of one pitched grid, each product checked before it is formed
-    const size_t capacity = (kScratchBytes - kWordsBytes) / (2 * sizeof(float));
+    // elements of one pitched grid, each product checked before it is formed;
+    // the scratch also holds three per-axis tables of the damping mask
+    const size_t tables = P->nz + P->nx + P->ny + 32;
+    if (tables > (kScratchBytes - kWordsBytes) / sizeof(float))
+        refuse(SIMWAVE_E_ARGUMENT, "grid extents exceed the allocation-free scratch");
+    const size_t capacity =
+        ((kScratchBytes - kWordsBytes) / sizeof(float) - tables) / 2;
     if (P->pitch > capacity || P->nx > capacity / P->pitch ||
         P->nz > capacity / (P->nx * P->pitch))
         refuse(SIMWAVE_E_ARGUMENT,
@@ -246,21 +252,35 @@ static int run(const simwave_problem* P, cudaStream_t st) {
                "layout not usable by the tiled kernel (use simwave_layout(): pitch a "
                "multiple of 4, lead + r a multiple of 32, arrays 16-byte aligned)");
 
-    // scratch: words, then C and Q; clear the words of the previous call
+    // scratch: words (zero box [0, 7), status [7], damping-table check [8]),
+    // then C, Q and the per-axis damping tables; clear the previous call's words
     unsigned char* base = scratch_address();
     int* words = reinterpret_cast<int*>(base);
     float* C = reinterpret_cast<float*>(base + kWordsBytes);
     float* Q = C + grid;
+    float* tabs = Q + grid;
     NA_CUDA(cudaMemsetAsync(words, 0, kWordsBytes, st));
     form_coefficients(vel, damp, C, Q, (long long)grid, (float)P->dt, st);
     NA_CUDA(cudaGetLastError());
     find_zero_box(Q, L, words, st);
     NA_CUDA(cudaGetLastError());
-    int box[7];
+    if (ctx.tm) {
+        damp_face_tables(damp, L, words, tabs, tabs + L.nz, tabs + L.nz + L.nx, words + 8, st);
+        NA_CUDA(cudaGetLastError());
+    }
+    int box[9];
     NA_CUDA(cudaMemcpyAsync(box, words, sizeof(box), cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaStreamSynchronize(st));
     const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2] && box[5] > box[4];
     for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
+    if (ctx.tm) {
+        ctx.damp = damp;
+        ctx.damp_tz = tabs;
+        ctx.damp_tx = tabs + L.nz;
+        ctx.damp_ty = tabs + L.nz + L.nx;
+        ctx.damp_faces_ok = good && box[8] == 0;
+        ctx.inv_dt = (float)(1.0 / P->dt);
+    }
     ctx.err = words + 7;
     ctx.coefC = C;
     ctx.coefQ = Q;

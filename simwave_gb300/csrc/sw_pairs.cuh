@@ -126,7 +126,8 @@ __device__ __forceinline__ float rcp_approx(float x) {
 
 // Weights duplicated into pairs (kernel parameters).
 struct PairWeights {
-    unsigned long long c2[kMaxRadius + 1], c1[kMaxRadius + 1], ih2[3], s1[3], one;
+    unsigned long long c2[kMaxRadius + 1], c1[kMaxRadius + 1], ih2[3], s1[3], one, two,
+        minus_one;
 };
 
 inline PairWeights pair_weights(const Weights<float>& W) {
@@ -145,6 +146,8 @@ inline PairWeights pair_weights(const Weights<float>& W) {
         P.s1[a] = dup(W.s1[a]);
     }
     P.one = dup(1.0f);
+    P.two = dup(2.0f);
+    P.minus_one = dup(-1.0f);
     return P;
 }
 

@@ -30,6 +30,7 @@
 #include "simwave_gb300.h"
 #include "sw_pairs.cuh"
 #include "sw_tiled.h"
+#include "sw_tma.cuh"
 
 namespace sw {
 
@@ -38,9 +39,6 @@ namespace {
 constexpr int kWarps = 8;
 constexpr int kThreads = 32 * kWarps;
 constexpr int kStages = 3;              // planes in flight per field
-constexpr unsigned kSpinLimit = 1u << 20;  // mbarrier polls before giving up
-
-__host__ __device__ constexpr int round4(int r) { return (r + 3) & ~3; }
 
 template <int R>
 struct Tile {
@@ -53,55 +51,6 @@ struct Tile {
     static constexpr int BYTES = ELEMS * 4;                   // one TMA box
     static constexpr int STRIDE = (ELEMS + 31) & ~31;         // 128 B aligned slots
 };
-
-// ---- PTX helpers -----------------------------------------------------------
-
-// The kernels' only shared memory: one dynamic region per CTA.
-extern __shared__ __align__(128) float4 sw_dyn_smem[];
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-// Bounded wait for phase `parity` of `bar`; returns false on expiry.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-    const unsigned addr = smem_addr(bar);
-    for (unsigned i = 0; i < kSpinLimit; i++) {
-        unsigned ok;
-        asm volatile(
-            "{\n"
-            ".reg .pred p;\n"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-            "selp.u32 %0, 1, 0, p;\n"
-            "}\n"
-            : "=r"(ok)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map,
-                                            unsigned long long* bar, int c0, int c1,
-                                            int c2, int c3) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_addr(dst)),
-        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
-        : "memory");
-}
 
 // ---- per-point coefficients --------------------------------------------------
 //
@@ -1284,16 +1233,42 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
             ctx.vec = true;
         }
     }
+    // tensor-memory kernel: orders up to 8, boxes of its x rows
+    ctx.tm = false;
+    const int pol = resolve_policy(kernel_policy(), r, vd);
+    if (r <= 4 && (L.lead + r) % 4 == 0 &&
+        (pol == SIMWAVE_POLICY_TMEM || pol == SIMWAVE_POLICY_TMEM_WIDE)) {
+        const int rows = tmem_rows(pol);
+        const int vw = 128 + 2 * round4(r), vh = rows + 2 * r;
+        CUtensorMap tu, trm;
+        if (encode_map(&tu, u_base, L, nslots, slot_stride, vw, vh) &&
+            (!vd || encode_map(&trm, den, L, 1, L.nz * L.plane, vw, vh))) {
+            if (!vd) trm = tu;
+            std::memcpy(ctx.map_u_tm, &tu, sizeof(tu));
+            std::memcpy(ctx.map_rho_tm, &trm, sizeof(trm));
+            ctx.tm = true;
+            ctx.tm_rows = rows;
+        }
+    }
     ctx.u_base = u_base;
     ctx.slot_stride = slot_stride;
     ctx.ok = true;
     return true;
 }
 
+int resolve_policy(int policy, int r, bool vd) {
+    return policy == SIMWAVE_POLICY_AUTO ? auto_policy(r, vd) : policy;
+}
+
 int tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, const float* up,
                   const float* vel, const float* den, const float* damp, const Layout& L,
                   const Weights<float>& W, float dt, float dt2, cudaStream_t st) {
-    const int policy = kernel_policy();
+    int policy = kernel_policy();
+    const int resolved = resolve_policy(policy, L.r, vd);
+    if (resolved == SIMWAVE_POLICY_TMEM || resolved == SIMWAVE_POLICY_TMEM_WIDE) {
+        if (tmem_launch(ctx, resolved, vd, un, uc, up, vel, den, L, W, st)) return resolved;
+        policy = SIMWAVE_POLICY_VEC_PACKED;  // the context was prepared for another kernel
+    }
     const bool aligned =
         (reinterpret_cast<uintptr_t>(vel) | reinterpret_cast<uintptr_t>(damp) |
          reinterpret_cast<uintptr_t>(un) | reinterpret_cast<uintptr_t>(up) |

@@ -1,0 +1,588 @@
+// sw_stencil_tmem.cu -- 3D float32 stencil, orders 2..8, whose z queues live
+// in tensor memory (sm_100 and later).
+//
+// Tiling as in the packed kernel of sw_stencil_tiled.cu: a CTA of XW warps
+// owns 128 (y) x XW (x) interior points and streams them along z over a chunk
+// of planes; lane l of warp w holds the y points y0 .. y0+3 (y0 = R + 128 bx +
+// 4 l) of the x row R + XW by + w. Per plane z:
+//   * the u tile and, with variable density, the density tile, each with an
+//     R-wide x/y halo, arrive in shared memory by TMA (cp.async.bulk.tensor,
+//     mbarrier completion), three planes deep: x and y derivatives;
+//   * the z derivatives come from per-thread rings of the 2R+1 planes
+//     z-R .. z+R held in tensor memory (TMEM): the thread's TMEM lane keeps
+//     one ring for u and one for the density, read with tcgen05.ld every
+//     plane; the ring head (plane z+R+1) is loaded from global memory a plane
+//     ahead and written with tcgen05.st into the slot plane z-R leaves. The
+//     rings cost no registers between planes, and the density's z term needs
+//     no per-point array of its own;
+//   * damping: where the mask is nonzero, its value comes from per-axis
+//     tables at points with exactly one axis outside the box where the mask
+//     is zero (tables taken from the mask's centre lines and checked on the
+//     device against every such point), and from the mask itself where two
+//     or three axes are outside (the layer's edges and corners); a mask that
+//     fails the check is read at every point outside the box. The update is
+//     written with t = damp C / dt:
+//       u_next = (2 - t) u - (1 - t) u_prev + C lap,
+//     the reference's 2/D u - N/D u_prev + value (dt^2/s)/D (D = 1 + q,
+//     N = 1 - q, q = damp dt / (2 s), C = (dt^2/s)/D, so 2/D = 2 - t and
+//     N/D = 1 - t); inside the box t = 0 and the arithmetic is the scalar
+//     update's;
+//   * arithmetic on 64-bit pairs (.f32x2): the derivative sums in the
+//     reference's order (c0 u first, then k = 1 .. R), the combine in the
+//     order y, x, z.
+// DRAM traffic per point update: u_cur, u_prev, C, density and u_next (20 B;
+// 16 B with constant density), plus the mask at the layer's edges and
+// corners.
+//
+// Every mbarrier wait is bounded; on expiry the CTA records an error code,
+// drains its outstanding copies (also bounded), frees its TMEM and returns.
+#include <cuda.h>
+
+#include <algorithm>
+#include <atomic>
+
+#include "simwave_gb300.h"
+#include "sw_pairs.cuh"
+#include "sw_tiled.h"
+#include "sw_tma.cuh"
+
+namespace sw {
+
+namespace {
+
+constexpr int kTmStages = 3;  // planes in flight per field
+
+__host__ __device__ constexpr int pow2_at_least(int n) {
+    int p = 32;
+    while (p < n) p *= 2;
+    return p;
+}
+
+template <int R, bool VD, int XW>
+struct TmTile {
+    static constexpr int HY = round4(R);
+    static constexpr int TW = 128 + 2 * HY;  // floats per tile row
+    static constexpr int TH = XW + 2 * R;    // tile rows
+    static constexpr int ELEMS = TW * TH;
+    static constexpr int BYTES = ELEMS * 4;  // one TMA box
+    static constexpr int STRIDE = (ELEMS + 31) & ~31;
+    static constexpr int NC = (2 * HY) / 4 + 1;  // float4 chunks of a y window
+    static constexpr int QN = 2 * R + 1;         // planes in a ring
+    static constexpr int QC = 4 * QN;            // TMEM columns of one ring
+    static constexpr int WC = (VD ? 2 : 1) * QC; // columns of one warp
+    static constexpr int NCOLS = pow2_at_least((XW / 4) * WC);  // per CTA
+    static constexpr int NF = VD ? 2 : 1;
+    static constexpr size_t SMEM = (size_t)NF * kTmStages * STRIDE * 4 + 64;
+};
+
+struct TmBox {  // interior box where the damping mask is zero
+    int z0, z1, x0, x1, y0, y1;
+};
+
+// The mask outside the zero box: per-axis tables (valid at points with one
+// axis outside the box when `ok`) and the mask itself.
+struct TmDamp {
+    const float* tz;
+    const float* tx;
+    const float* ty;
+    const float* damp;
+    int ok;
+};
+
+__device__ __forceinline__ P2 pair_of(unsigned a, unsigned b) {
+    P2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "r"(a), "r"(b));
+    return r;
+}
+__device__ __forceinline__ void halves(P2 p, unsigned& a, unsigned& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(a), "=r"(b) : "l"(p.v));
+}
+__device__ __forceinline__ void tmem_st_v4(unsigned taddr, V4 v) {
+    unsigned a, b, c, d;
+    halves(v.lo, a, b);
+    halves(v.hi, c, d);
+    tmem_st4(taddr, a, b, c, d);
+}
+// plane slot s of a ring loaded into r
+__device__ __forceinline__ V4 ring_at(const unsigned* r, int s) {
+    return {pair_of(r[4 * s], r[4 * s + 1]), pair_of(r[4 * s + 2], r[4 * s + 3])};
+}
+
+template <int R, bool VD, int XW, int MINB>
+__global__ void __launch_bounds__(32 * XW, MINB)
+stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
+               const __grid_constant__ CUtensorMap map_rho, float* un,
+               const float* __restrict__ uc, const float* up,
+               const float* __restrict__ coefC, const float* __restrict__ den, TmDamp F,
+               Layout L, PairWeights PW, float inv_dt, int slot_cur, int zchunk, TmBox zb,
+               int* __restrict__ err) {
+    using TT = TmTile<R, VD, XW>;
+    constexpr int HY = TT::HY, TW = TT::TW, NC = TT::NC, QN = TT::QN, QC = TT::QC;
+    constexpr int NF = TT::NF;
+    float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [NF][stages][STRIDE]
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(tiles + NF * kTmStages * TT::STRIDE);
+    int* words = reinterpret_cast<int*>(bars + kTmStages);
+    int& s_abort = words[0];
+    unsigned& s_tmem = *reinterpret_cast<unsigned*>(words + 1);
+    if (smem_addr(tiles) & 127) {  // layout assumption broken: refuse
+        if (threadIdx.x == 0) atomicExch(err, SIMWAVE_E_ARGUMENT);
+        return;
+    }
+    // an earlier launch already failed: read once, so every warp of the CTA
+    // leaves together (the TMEM allocation below is the CTA's)
+    if (threadIdx.x == 0) s_abort = *(volatile int*)err;
+    __syncthreads();
+    if (s_abort) return;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int yb = R + blockIdx.x * 128;
+    const int y0 = yb + 4 * lane;
+    const int x = R + blockIdx.y * XW + warp;
+    const int zbeg = R + blockIdx.z * zchunk;
+    const int zend = min(zbeg + zchunk, (int)L.nz - R);
+    if (zbeg >= zend) return;  // uniform over the CTA, before any allocation
+    const int ylim = (int)L.ny - R;
+    const bool any = x < (int)L.nx - R && y0 < ylim;
+    const bool full = any && y0 + 3 < ylim;
+    const int off = x * (int)L.pitch + (int)L.lead + y0;
+    // threads past the interior load from the last interior row / chunk
+    // (inside the grid) instead of selecting zeros; only their stores are
+    // masked
+    const int xl = min(x, (int)L.nx - R - 1);
+    const int yl = min(y0, R + 4 * ((ylim - 1 - R) / 4));
+    const int offl = xl * (int)L.pitch + (int)L.lead + yl;
+    const int col0 = (int)L.lead + yb - HY;
+    const int row0 = blockIdx.y * XW;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTmStages; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 0) tmem_alloc(&s_tmem, TT::NCOLS);
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
+    // this warp's columns in its lane quadrant: the u ring, then the density ring
+    const unsigned tbase = s_tmem;
+    const unsigned tu =
+        tbase + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)((warp >> 2) * TT::WC);
+    const unsigned tr = tu + QC;
+
+    auto issue = [&](int plane, int stage) {
+        mbar_expect_tx(&bars[stage], NF * TT::BYTES);
+        tma_load_4d(tiles + stage * TT::STRIDE, &map_u, &bars[stage], col0, row0, plane,
+                    slot_cur);
+        if (VD)
+            tma_load_4d(tiles + (kTmStages + stage) * TT::STRIDE, &map_rho, &bars[stage], col0,
+                        row0, plane, 0);
+    };
+    int issued = 0;
+    if (threadIdx.x == 0)
+        for (; issued < kTmStages && zbeg + issued < zend; issued++)
+            issue(zbeg + issued, issued);
+
+    P2 w2[R + 1], w1[R + 1];
+#pragma unroll
+    for (int k = 0; k <= R; k++) {
+        w2[k].v = PW.c2[k];
+        w1[k].v = PW.c1[k];
+    }
+    auto vs = [&](int k, V4 a, V4 acc) -> V4 { return vfma(w2[k], a, acc); };
+    auto vw = [&](bool first, int k, V4 a, V4 acc) -> V4 {
+        return first ? vmul(w1[k], a) : vfma(w1[k], a, acc);
+    };
+
+    // rings: plane p sits in slot (p - zbeg + R) mod QN
+#pragma unroll
+    for (int j = 0; j < QN; j++) {
+        const long long pz = (long long)(zbeg - R + j) * L.plane + offl;
+        tmem_st_v4(tu + 4 * j, ldg_v4(uc + pz, true));
+        if (VD) tmem_st_v4(tr + 4 * j, ldg_v4(den + pz, true));
+    }
+    tmem_wait_st();
+
+    // damping state of the thread's column
+    const bool xin = x >= zb.x0 && x < zb.x1;
+    const float txv = F.ok ? __ldg(F.tx + xl) : 0.f;
+    unsigned yinm = 0;
+    float tyv[4];
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+        const int yy = min(y0 + v, (int)L.ny - 1);
+        yinm |= (unsigned)(yy >= zb.y0 && yy < zb.y1) << v;
+        tyv[v] = F.ok ? __ldg(F.ty + yy) : 0.f;
+    }
+    const bool colin = xin && yinm == 15u;
+
+    // per-point operands of the next plane, fetched a plane ahead
+    V4 nprev, ncoef, ng = vzero();
+    float ntz = 0.f;
+    bool nbox = true;
+    unsigned nneed = 0;
+    auto fetch = [&](int zz) {
+        const long long p = (long long)zz * L.plane + offl;
+        nprev = ld_v4(up + p, true);
+        ncoef = ldg_v4(coefC + p, true);
+        const bool zin = zz >= zb.z0 && zz < zb.z1;
+        nbox = zin && colin;
+        nneed = 0;
+        if (!nbox) {
+            ntz = F.ok ? __ldg(F.tz + zz) : 0.f;
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int out = !zin + !xin + !((yinm >> v) & 1u);
+                nneed |= (unsigned)(out >= 2 || (!F.ok && out >= 1)) << v;
+            }
+            ng = ldg_v4(F.damp + p, nneed != 0);
+        }
+    };
+    fetch(zbeg);
+    int aborted_at = -1;
+    long long zoff = (long long)zbeg * L.plane;
+
+    auto plane_step = [&](const int z, const int J, const int m) -> bool {
+        constexpr bool kStatic = QN % kTmStages == 0;
+        const int it = QN * m + J;
+        const int stage = kStatic ? J % kTmStages : it % kTmStages;
+        const unsigned parity = kStatic ? (unsigned)(((QN / kTmStages) * m + J / kTmStages) & 1)
+                                        : (unsigned)((it / kTmStages) & 1);
+        auto slot = [&](int d) { return (J + R + d) % QN; };  // plane z + d
+        const bool zin = z >= zb.z0 && z < zb.z1;
+        const V4 vprev = nprev, vcoef = ncoef, vg = ng;
+        const bool inbox = nbox;
+        const unsigned need = nneed;
+        const float vtz = ntz;
+
+        unsigned ur[QC];
+        tmem_ld_cols<QC>(tu, ur);  // u ring (asynchronous)
+        V4 hu = vzero(), hr = vzero();
+        const bool more = z + 1 < zend;
+        if (more) {  // ring heads (plane z+R+1) and the next plane's operands
+            const long long ph = zoff + (long long)(R + 1) * L.plane + offl;
+            hu = ldg_v4(uc + ph, true);
+            if (VD) hr = ldg_v4(den + ph, true);
+            fetch(z + 1);
+        }
+        const long long pz = zoff + off;
+        zoff += L.plane;
+
+        // z axis of u from the ring (c0 u first, then k = 1 .. R)
+        tmem_wait_ld<QC>(ur);
+        const V4 u0 = ring_at(ur, slot(0));
+        V4 sdz = vmul(w2[0], u0), fuz = vzero();
+#pragma unroll
+        for (int k = 1; k <= R; k++) {
+            const V4 a = ring_at(ur, slot(k)), b = ring_at(ur, slot(-k));
+            sdz = vs(k, vadd(a, b), sdz);
+            if (VD) fuz = vw(k == 1, k, vsub(a, b), fuz);
+        }
+
+        // warp-uniform, so the warp's tcgen05 operations stay converged
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[stage], parity));
+        if (!ok) s_abort = 1;
+        if (ok) {
+            const float* tus = tiles + stage * TT::STRIDE + (warp + R) * TW + 4 * lane;
+            const float* trs =
+                tiles + (kTmStages + stage) * TT::STRIDE + (warp + R) * TW + 4 * lane;
+            // y axis of u on pairs: even offsets straight from the 16-byte
+            // loads, odd offsets repacked once
+            V4 sdy, fuy;
+            {
+                P2 ev[2 * NC], od[2 * NC - 1];
+                YWindow<NC>::load(tus, ev, od);
+                P2 s[2], g[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    s[h] = mul2(w2[0], h ? u0.hi : u0.lo);
+#pragma unroll
+                    for (int k = 1; k <= R; k++) {
+                        const P2 a = YWindow<NC>::at(ev, od, HY + 2 * h + k);
+                        const P2 b = YWindow<NC>::at(ev, od, HY + 2 * h - k);
+                        s[h] = fma2(w2[k], add2(a, b), s[h]);
+                        if (VD)
+                            g[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), g[h]);
+                    }
+                }
+                sdy = {s[0], s[1]};
+                if (VD) fuy = {g[0], g[1]};
+            }
+            // x axis of u: rows x +- k of the tile
+            V4 sdx = vmul(w2[0], u0), fux = vzero();
+#pragma unroll
+            for (int k = 1; k <= R; k++) {
+                const V4 a = lds_v4(tus + k * TW + HY);
+                const V4 b = lds_v4(tus - k * TW + HY);
+                sdx = vs(k, vadd(a, b), sdx);
+                if (VD) fux = vw(k == 1, k, vsub(a, b), fux);
+            }
+            // lap = y / hy^2 + x / hx^2 + z / hz^2
+            V4 lap = vmul({PW.ih2[2]}, sdy);
+            lap = vfma({PW.ih2[1]}, sdx, lap);
+            lap = vfma({PW.ih2[0]}, sdz, lap);
+            if (VD) {
+                unsigned rr[QC];
+                tmem_ld_cols<QC>(tr, rr);  // density ring (asynchronous)
+                V4 rho0, fry, frx = vzero();
+                {
+                    P2 ev[2 * NC], od[2 * NC - 1];
+                    YWindow<NC>::load(trs, ev, od);
+                    rho0 = {ev[HY / 2], ev[HY / 2 + 1]};
+                    P2 g[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+#pragma unroll
+                        for (int k = 1; k <= R; k++) {
+                            const P2 a = YWindow<NC>::at(ev, od, HY + 2 * h + k);
+                            const P2 b = YWindow<NC>::at(ev, od, HY + 2 * h - k);
+                            g[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), g[h]);
+                        }
+                    }
+                    fry = {g[0], g[1]};
+                }
+#pragma unroll
+                for (int k = 1; k <= R; k++) {
+                    const V4 a = lds_v4(trs + k * TW + HY);
+                    const V4 b = lds_v4(trs - k * TW + HY);
+                    frx = vw(k == 1, k, vsub(a, b), frx);
+                }
+                tmem_wait_ld<QC>(rr);
+                V4 frz = vzero();
+#pragma unroll
+                for (int k = 1; k <= R; k++)
+                    frz = vw(k == 1, k, vsub(ring_at(rr, slot(k)), ring_at(rr, slot(-k))), frz);
+                // cross = (fy gy / (4 hy^2) + fx gx / (4 hx^2) + fz gz / (4 hz^2))
+                V4 cross = vmul({PW.s1[2]}, {mul2(fuy.lo, fry.lo), mul2(fuy.hi, fry.hi)});
+                cross = vfma({PW.s1[1]}, {mul2(fux.lo, frx.lo), mul2(fux.hi, frx.hi)}, cross);
+                cross = vfma({PW.s1[0]}, {mul2(fuz.lo, frz.lo), mul2(fuz.hi, frz.hi)}, cross);
+                const float4 rr4 = to_f4(rho0);
+                const V4 inv = from_f4(make_float4(rcp_approx(rr4.x), rcp_approx(rr4.y),
+                                                   rcp_approx(rr4.z), rcp_approx(rr4.w)));
+                // lap -= cross / rho
+                lap = {fma2(sub2({0ull}, cross.lo), inv.lo, lap.lo),
+                       fma2(sub2({0ull}, cross.hi), inv.hi, lap.hi)};
+            }
+            // a = (2 - t) u - (1 - t) u_prev, t = damp C / dt (0 in the box)
+            V4 a;
+            if (inbox) {
+                const P2 m1{PW.minus_one};
+                a = {fma2(m1, vprev.lo, add2(u0.lo, u0.lo)), fma2(m1, vprev.hi, add2(u0.hi, u0.hi))};
+            } else {
+                float d[4];
+                const float4 g4 = to_f4(vg);
+                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const float face = (!zin ? vtz : 0.f) + (!xin ? txv : 0.f) +
+                                       (((yinm >> v) & 1u) ? 0.f : tyv[v]);
+                    d[v] = ((need >> v) & 1u) ? gg[v] : face;
+                }
+                const V4 dv = from_f4(make_float4(d[0], d[1], d[2], d[3]));
+                const P2 idt = pk(inv_dt, inv_dt);
+                const V4 t = {mul2(mul2(dv.lo, vcoef.lo), idt), mul2(mul2(dv.hi, vcoef.hi), idt)};
+                const P2 one{PW.one}, two{PW.two};
+                a = {fma2(sub2(t.lo, one), vprev.lo, mul2(sub2(two, t.lo), u0.lo)),
+                     fma2(sub2(t.hi, one), vprev.hi, mul2(sub2(two, t.hi), u0.hi))};
+            }
+            const V4 out = {fma2(lap.lo, vcoef.lo, a.lo), fma2(lap.hi, vcoef.hi, a.hi)};
+            if (full) {
+                *reinterpret_cast<ulonglong2*>(un + pz) = make_ulonglong2(out.lo.v, out.hi.v);
+            } else if (any) {
+                const float4 o = to_f4(out);
+                const float ov[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    if (y0 + v < ylim) un[pz + v] = ov[v];
+            }
+        }
+        // ring heads into the slot plane z - R leaves
+        if (more) {
+            tmem_st_v4(tu + 4 * slot(-R), hu);
+            if (VD) tmem_st_v4(tr + 4 * slot(-R), hr);
+        }
+        __syncthreads();  // the stage is free again; abort is uniform here
+        if (s_abort) {
+            aborted_at = it;
+            return false;
+        }
+        if (threadIdx.x == 0 && z + kTmStages < zend) {
+            issue(z + kTmStages, stage);
+            issued++;
+        }
+        tmem_wait_st();  // the next plane's ring loads see the heads
+        return true;
+    };
+
+    for (int m = 0; zbeg + QN * m < zend; m++) {
+#pragma unroll
+        for (int J = 0; J < QN; J++) {
+            const int z = zbeg + QN * m + J;
+            if (z >= zend || !plane_step(z, J, m)) break;
+        }
+        if (aborted_at >= 0) break;
+    }
+    if (aborted_at >= 0 && threadIdx.x == 0) {
+        atomicExch(err, SIMWAVE_E_TIMEOUT);
+        for (int p = aborted_at; p < issued; p++)
+            mbar_wait(&bars[p % kTmStages], (unsigned)((p / kTmStages) & 1));
+    }
+    // every warp is done with TMEM before the allocating warp frees it
+    tmem_wait_st();
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
+    if (warp == 0) tmem_dealloc(tbase, TT::NCOLS);
+}
+
+// ---- damping tables ------------------------------------------------------------
+
+// tz[i] = damp(i, xc, yc), tx[j] = damp(zc, j, yc), ty[k] = damp(zc, xc, k) at
+// the centre (zc, xc, yc) of the zero box `box` (device words z0, z1, x0, x1,
+// y0, y1).
+__global__ void damp_tables(const float* __restrict__ damp, Layout L, const int* box,
+                            float* tz, float* tx, float* ty) {
+    const int zc = (box[0] + box[1]) / 2, xc = (box[2] + box[3]) / 2, yc = (box[4] + box[5]) / 2;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+         t < L.nz + L.nx + L.ny; t += (long long)gridDim.x * blockDim.x) {
+        if (t < L.nz)
+            tz[t] = damp[L.at3(t, xc, yc)];
+        else if (t < L.nz + L.nx)
+            tx[t - L.nz] = damp[L.at3(zc, t - L.nz, yc)];
+        else
+            ty[t - L.nz - L.nx] = damp[L.at3(zc, xc, t - L.nz - L.nx)];
+    }
+}
+
+// Checks every interior point with exactly one axis outside the zero box
+// against that axis' table; a mismatch sets *bad.
+__global__ void damp_tables_verify(const float* __restrict__ damp, Layout L, const int* box,
+                                   const float* __restrict__ tz, const float* __restrict__ tx,
+                                   const float* __restrict__ ty, int* bad) {
+    const int r = L.r;
+    const long long ny = L.ny - 2 * r, nx = L.nx - 2 * r, nz = L.nz - 2 * r;
+    const long long total = nz * nx * ny;
+    int mismatch = 0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = r + (int)(t % ny), j = r + (int)((t / ny) % nx), i = r + (int)(t / (ny * nx));
+        const bool zo = i < box[0] || i >= box[1], xo = j < box[2] || j >= box[3],
+                   yo = k < box[4] || k >= box[5];
+        if ((int)zo + (int)xo + (int)yo != 1) continue;
+        const float want = zo ? tz[i] : (xo ? tx[j] : ty[k]);
+        mismatch |= damp[L.at3(i, j, k)] != want;
+    }
+    if (__syncthreads_or(mismatch) && threadIdx.x == 0) atomicOr(bad, 1);
+}
+
+struct TmDeviceInfo {
+    int sms = 0;
+};
+
+int tm_sms() {
+    static std::atomic<int> sms[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!sms[dev & 63]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev & 63] = std::max(v, 1);
+    }
+    return sms[dev & 63];
+}
+
+// z chunk length: fill the machine in whole waves, counting the 2R-plane
+// warm-up of every chunk as the cost of splitting.
+int tm_chunk(int ty, int tx, int nzi, int R, int per_sm) {
+    const long long slots = (long long)std::max(per_sm, 1) * tm_sms();
+    int best = 1;
+    double best_cost = 1e300;
+    for (int zs = 1; zs <= 32 && zs <= nzi; zs++) {
+        const long long ctas = (long long)ty * tx * zs;
+        const long long waves = (ctas + slots - 1) / slots;
+        const int chunk = (nzi + zs - 1) / zs;
+        const double cost = (double)waves * (chunk + 2.0 * R * 0.5);
+        if (cost < best_cost * 0.999) {
+            best_cost = cost;
+            best = zs;
+        }
+    }
+    return (nzi + best - 1) / best;
+}
+
+// Shared memory of a CTA: the tiles, padded so that no more than MINB CTAs
+// fit on an SM (their TMEM allocations must fit the SM's 512 columns).
+template <int R, bool VD, int XW, int MINB>
+size_t tm_smem() {
+    using TT = TmTile<R, VD, XW>;
+    static_assert(MINB * TT::NCOLS <= 512, "TMEM columns of the resident CTAs");
+    const size_t per_sm = 228 * 1024;
+    const size_t floor = per_sm / (MINB + 1) + 1024;
+    return std::max(TT::SMEM, floor);
+}
+
+template <int R, bool VD, int XW, int MINB>
+void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
+               const float* den, const Layout& L, const Weights<float>& W,
+               const TiledContext& ctx, cudaStream_t st) {
+    auto kernel = stencil3d_tmem<R, VD, XW, MINB>;
+    static std::atomic<bool> configured[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t smem = tm_smem<R, VD, XW, MINB>();
+    if (!configured[dev & 63]) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured[dev & 63] = true;
+    }
+    const int ty = (int)((L.ny - 2 * R + 127) / 128);
+    const int tx = (int)((L.nx - 2 * R + XW - 1) / XW);
+    const int nzi = (int)(L.nz - 2 * R);
+    const int chunk = tm_chunk(ty, tx, nzi, R, MINB);
+    const int zsplit = (nzi + chunk - 1) / chunk;
+    const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
+    TmBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
+             ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
+    TmDamp F{ctx.damp_tz, ctx.damp_tx, ctx.damp_ty, ctx.damp, ctx.damp_faces_ok};
+    PairWeights PW = pair_weights(W);
+    dim3 grid(ty, tx, zsplit);
+    kernel<<<grid, 32 * XW, smem, st>>>(
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_u_tm),
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), un, uc, up, coefC, den, F, L, PW,
+        ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
+}
+
+}  // namespace
+
+int tmem_rows(int policy) { return policy == SIMWAVE_POLICY_TMEM_WIDE ? 16 : 8; }
+
+void damp_face_tables(const float* damp, const Layout& L, const int* box, float* tz,
+                      float* tx, float* ty, int* bad, cudaStream_t st) {
+    cudaMemsetAsync(bad, 0, sizeof(int), st);
+    damp_tables<<<(unsigned)((L.nz + L.nx + L.ny + 255) / 256), 256, 0, st>>>(damp, L, box, tz,
+                                                                            tx, ty);
+    damp_tables_verify<<<tm_sms() * 4, 256, 0, st>>>(damp, L, box, tz, tx, ty, bad);
+}
+
+bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const float* uc,
+                 const float* up, const float* coefC, const float* den, const Layout& L,
+                 const Weights<float>& W, cudaStream_t st) {
+    if (!ctx.tm || L.r > 4 || !ctx.damp || !ctx.damp_tz) return false;
+    const bool wide = policy == SIMWAVE_POLICY_TMEM_WIDE;
+    if (wide != (ctx.tm_rows == 16)) return false;
+#define SW_TM(RR)                                                                  \
+    case RR:                                                                       \
+        if (vd) {                                                                  \
+            if (wide) launch_tm<RR, true, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st);  \
+            else launch_tm<RR, true, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);        \
+        } else {                                                                   \
+            if (wide) launch_tm<RR, false, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st); \
+            else launch_tm<RR, false, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);       \
+        }                                                                          \
+        return true;
+    switch (L.r) { SW_TM(1) SW_TM(2) SW_TM(3) SW_TM(4) }
+#undef SW_TM
+    return false;
+}
+
+}  // namespace sw

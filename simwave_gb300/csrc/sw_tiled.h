@@ -23,6 +23,17 @@ struct TiledContext {
     const float* coefQ = nullptr;
     const float* coefGz = nullptr; // density z term (variable density), or null
     void* scratch = nullptr;       // the run's coefficient/zero-box scratch
+    // kernel with its z queues in tensor memory (sw_stencil_tmem.cu)
+    alignas(64) unsigned char map_u_tm[128];   // boxes of tm_rows x rows
+    alignas(64) unsigned char map_rho_tm[128];
+    bool tm = false;               // descriptors encoded
+    int tm_rows = 8;               // x rows per CTA (8 or 16)
+    const float* damp = nullptr;   // the damping mask (pitched like u)
+    const float* damp_tz = nullptr;  // mask along the zero box's centre lines
+    const float* damp_tx = nullptr;
+    const float* damp_ty = nullptr;
+    int damp_faces_ok = 0;         // tables match every one-axis-outside point
+    float inv_dt = 0.f;
 };
 
 // Encodes the descriptors; false when the layout or alignment does not suit
@@ -105,6 +116,21 @@ bool wants_density_z(const Layout& L, bool vd);
 
 int kernel_policy();
 void set_kernel_policy(int policy);
+// The SIMWAVE_POLICY_* the tiled launch resolves `policy` to for radius r.
+int resolve_policy(int policy, int r, bool vd);
+
+// Tensor-memory kernel (sw_stencil_tmem.cu): x rows per CTA of a policy;
+// the launch, false when the context or the radius does not suit it (then
+// nothing is launched).
+int tmem_rows(int policy);
+bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const float* uc,
+                 const float* up, const float* coefC, const float* den, const Layout& L,
+                 const Weights<float>& W, cudaStream_t st);
+// Per-axis tables of the mask along the zero box's centre lines (device
+// arrays of nz, nx, ny floats) and their check: *bad (device) becomes
+// nonzero if a point with one axis outside the box differs from its table.
+void damp_face_tables(const float* damp, const Layout& L, const int* box, float* tz,
+                      float* tx, float* ty, int* bad, cudaStream_t st);
 
 void find_zero_box(const float* damp, const Layout& L, int* box, cudaStream_t st);
 

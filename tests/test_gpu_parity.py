@@ -162,7 +162,7 @@ def test_repeated_calls_are_deterministic():
 
 POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3,
             "vec_smemq": 4, "vec_2cta_rot": 5, "vec_1cta_rot": 6, "vec_packed": 7,
-            "vec_packed_1cta": 8}
+            "vec_packed_1cta": 8, "tmem": 9, "tmem_wide": 10}
 
 
 @pytest.mark.parametrize("policy", list(POLICIES))
@@ -247,3 +247,42 @@ def test_fused_step_sources_across_tiles(order, vd):
     ru, rrec = port_forward(kw)
     assert_close(dp.u_full_numpy(), ru, np.float32, "fused-step wavefield")
     assert_close(dp.shot_record_numpy(), rrec, np.float32, "fused-step shot record")
+
+
+@pytest.mark.parametrize("policy", ["tmem", "tmem_wide"])
+@pytest.mark.parametrize("mask", ["perturbed_faces", "uniform", "none"])
+def test_tmem_kernel_damping_masks(policy, mask):
+    """The tensor-memory kernel takes the damping mask from per-axis tables
+    where one axis is outside the zero box, checked on the device against
+    the mask: a mask whose faces differ from its centre lines (read at every
+    point instead), a uniform mask (no zero box) and no damping layer (the
+    box is the whole grid) all match the oracle."""
+    from simwave_gb300.backend import _lib
+    from simwave_gb300.device import DeviceProblem
+    bc = ("null_dirichlet", "null_neumann", "none", "null_dirichlet",
+          "null_neumann", "none")
+    kw = random_problem(sw, 3, 8, True, bc, 0, shape=(34, 45, 47), tf=0.04, seed=3,
+                        nrec=5, damping=0.0 if mask == "none" else 80.0)
+    damp = kw["damping_mask"].copy()
+    rng = np.random.default_rng(7)
+    if mask == "perturbed_faces":
+        # points of the z, x and y faces (layer 4..11 and the far side), of
+        # an edge and of a corner differ from the centre lines
+        for idx in ((5, 30, 30), (50, 20, 25), (30, 6, 30), (30, 60, 40), (25, 30, 6),
+                    (25, 30, 62), (6, 6, 30), (5, 5, 5)):
+            damp[idx] *= np.float32(1.0 + 0.5 * rng.random())
+    elif mask == "uniform":
+        damp[:] = np.float32(0.3)
+    kw["damping_mask"] = damp
+    dp = DeviceProblem(kw)
+    lib = _lib.load()
+    assert lib.simwave_set_kernel_policy(POLICIES[policy]) == 0
+    try:
+        st = dp.run()
+        dp.status()
+    finally:
+        lib.simwave_set_kernel_policy(0)
+    assert st["stencil_kernel"] == POLICIES[policy]
+    ru, rrec = port_forward(kw)
+    assert_close(dp.u_full_numpy(), ru, np.float32, "wavefield")
+    assert_close(dp.shot_record_numpy(), rrec, np.float32, "shot record")
