@@ -1176,6 +1176,8 @@ void form_density_z(const float* den, float* gz, const Layout& L, const Weights<
 bool wants_density_z(const Layout& L, bool vd) {
     int p = kernel_policy();
     if (p == SIMWAVE_POLICY_AUTO) p = auto_policy(L.r, vd);
+    if ((p == SIMWAVE_POLICY_TMEM || p == SIMWAVE_POLICY_TMEM_WIDE) && L.r <= 4)
+        return vd && L.dim == 3 && tmem_wants_density_z();
     return vd && L.dim == 3 && L.r <= 8 &&
            (p == SIMWAVE_POLICY_VEC_PACKED || p == SIMWAVE_POLICY_VEC_PACKED_1CTA);
 }

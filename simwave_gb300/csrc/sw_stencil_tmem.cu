@@ -40,6 +40,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdio>
+#include <cstdlib>
 
 #include "simwave_gb300.h"
 #include "sw_pairs.cuh"
@@ -58,7 +60,7 @@ __host__ __device__ constexpr int pow2_at_least(int n) {
     return p;
 }
 
-template <int R, bool VD, int XW>
+template <int R, bool VD, int XW, int UQ = 1, int RZ = 0>
 struct TmTile {
     static constexpr int HY = round4(R);
     static constexpr int TW = 128 + 2 * HY;  // floats per tile row
@@ -69,10 +71,12 @@ struct TmTile {
     static constexpr int NC = (2 * HY) / 4 + 1;  // float4 chunks of a y window
     static constexpr int QN = 2 * R + 1;         // planes in a ring
     static constexpr int QC = 4 * QN;            // TMEM columns of one ring
-    static constexpr int WC = (VD ? 2 : 1) * QC; // columns of one warp
+    // TMEM columns of one warp: the u ring and / or the density ring
+    static constexpr int WC = (UQ == 1 ? QC : 0) + ((VD && RZ == 0) ? QC : 0);
     static constexpr int NCOLS = pow2_at_least((XW / 4) * WC);  // per CTA
     static constexpr int NF = VD ? 2 : 1;
-    static constexpr size_t SMEM = (size_t)NF * kTmStages * STRIDE * 4 + 64;
+    static constexpr size_t SMEM = (size_t)NF * kTmStages * STRIDE * 4 +
+                                   ((VD && RZ == 1) ? (size_t)QN * 32 * XW * 16 : 0) + 64;
 };
 
 struct TmBox {  // interior box where the damping mask is zero
@@ -108,20 +112,35 @@ __device__ __forceinline__ V4 ring_at(const unsigned* r, int s) {
     return {pair_of(r[4 * s], r[4 * s + 1]), pair_of(r[4 * s + 2], r[4 * s + 3])};
 }
 
-template <int R, bool VD, int XW, int MINB>
+// Where the z derivatives come from (template switches of the kernel):
+//   UQ  u queue: 0 registers (slots static in the unrolled plane loop),
+//       1 a ring in tensor memory;
+//   RZ  density z term: 0 a ring in tensor memory, 1 a per-thread ring in
+//       shared memory, 2 the per-point array gz = s1_z sum_k c1_k (rho(z+k)
+//       - rho(z-k)) formed once per run (4 B more per point), 3 a queue in
+//       registers.
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ>
 __global__ void __launch_bounds__(32 * XW, MINB)
 stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                const __grid_constant__ CUtensorMap map_rho, float* un,
                const float* __restrict__ uc, const float* up,
-               const float* __restrict__ coefC, const float* __restrict__ den, TmDamp F,
-               Layout L, PairWeights PW, float inv_dt, int slot_cur, int zchunk, TmBox zb,
-               int* __restrict__ err) {
-    using TT = TmTile<R, VD, XW>;
+               const float* __restrict__ coefC, const float* __restrict__ den,
+               const float* __restrict__ gz, TmDamp F, Layout L, PairWeights PW, float inv_dt,
+               int slot_cur, int zchunk, TmBox zb, int* __restrict__ err) {
+    using TT = TmTile<R, VD, XW, UQ, RZ>;
     constexpr int HY = TT::HY, TW = TT::TW, NC = TT::NC, QN = TT::QN, QC = TT::QC;
     constexpr int NF = TT::NF;
+    constexpr int NT = 32 * XW;
+    constexpr bool TM_U = UQ == 1;
+    constexpr bool TM_R = VD && RZ == 0;
+    constexpr bool SM_R = VD && RZ == 1;
+    constexpr bool GZ_R = VD && RZ == 2;
+    constexpr bool RG_R = VD && RZ == 3;
+    constexpr bool USE_TMEM = TM_U || TM_R;
     float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [NF][stages][STRIDE]
+    float4* sq_base = reinterpret_cast<float4*>(tiles + NF * kTmStages * TT::STRIDE);
     unsigned long long* bars =
-        reinterpret_cast<unsigned long long*>(tiles + NF * kTmStages * TT::STRIDE);
+        reinterpret_cast<unsigned long long*>(sq_base + (SM_R ? QN * NT : 0));
     int* words = reinterpret_cast<int*>(bars + kTmStages);
     int& s_abort = words[0];
     unsigned& s_tmem = *reinterpret_cast<unsigned*>(words + 1);
@@ -146,13 +165,13 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     const int ylim = (int)L.ny - R;
     const bool any = x < (int)L.nx - R && y0 < ylim;
     const bool full = any && y0 + 3 < ylim;
-    const int off = x * (int)L.pitch + (int)L.lead + y0;
     // threads past the interior load from the last interior row / chunk
     // (inside the grid) instead of selecting zeros; only their stores are
     // masked
     const int xl = min(x, (int)L.nx - R - 1);
     const int yl = min(y0, R + 4 * ((ylim - 1 - R) / 4));
     const int offl = xl * (int)L.pitch + (int)L.lead + yl;
+    const int dstore = (x * (int)L.pitch + (int)L.lead + y0) - offl;  // store offset
     const int col0 = (int)L.lead + yb - HY;
     const int row0 = blockIdx.y * XW;
 
@@ -161,15 +180,15 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
-    if (warp == 0) tmem_alloc(&s_tmem, TT::NCOLS);
-    tmem_fence_before_sync();
+    if (USE_TMEM && warp == 0) tmem_alloc(&s_tmem, TT::NCOLS);
+    if (USE_TMEM) tmem_fence_before_sync();
     __syncthreads();
-    tmem_fence_after_sync();
+    if (USE_TMEM) tmem_fence_after_sync();
     // this warp's columns in its lane quadrant: the u ring, then the density ring
-    const unsigned tbase = s_tmem;
+    const unsigned tbase = USE_TMEM ? s_tmem : 0u;
     const unsigned tu =
         tbase + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)((warp >> 2) * TT::WC);
-    const unsigned tr = tu + QC;
+    const unsigned tr = tu + (TM_U ? QC : 0);
 
     auto issue = [&](int plane, int stage) {
         mbar_expect_tx(&bars[stage], NF * TT::BYTES);
@@ -195,53 +214,59 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         return first ? vmul(w1[k], a) : vfma(w1[k], a, acc);
     };
 
-    // rings: plane p sits in slot (p - zbeg + R) mod QN
+    // queues and rings: plane p sits in slot (p - zbeg + R) mod QN
+    V4 qu[TM_U ? 1 : QN];
+    V4 qr[RG_R ? QN : 1];
+    float4* sq = sq_base + threadIdx.x;
+    {
+        const float* pu = uc + (long long)(zbeg - R) * L.plane + offl;
+        const float* pr = den + (long long)(zbeg - R) * L.plane + offl;
 #pragma unroll
-    for (int j = 0; j < QN; j++) {
-        const long long pz = (long long)(zbeg - R + j) * L.plane + offl;
-        tmem_st_v4(tu + 4 * j, ldg_v4(uc + pz, true));
-        if (VD) tmem_st_v4(tr + 4 * j, ldg_v4(den + pz, true));
+        for (int j = 0; j < QN; j++) {
+            const V4 a = ldg_v4(pu, true);
+            if (TM_U) tmem_st_v4(tu + 4 * j, a);
+            else qu[j] = a;
+            if (TM_R) tmem_st_v4(tr + 4 * j, ldg_v4(pr, true));
+            if (SM_R) sts_v4(sq + j * NT, ldg_v4(pr, true));
+            if (RG_R) qr[j] = ldg_v4(pr, true);
+            pu += L.plane;
+            pr += L.plane;
+        }
     }
-    tmem_wait_st();
+    if (USE_TMEM) tmem_wait_st();
 
-    // damping state of the thread's column
+    // damping of the thread's points outside the zero box, looked up when a
+    // plane needs it: with z inside the box, from the x or y table where
+    // exactly one of x, y is outside, from the mask where both are (gzi);
+    // with z outside, from the z table, or from the mask where x or y is
+    // outside too (gzo). A mask that failed the table check is read at every
+    // point outside the box.
     const bool xin = x >= zb.x0 && x < zb.x1;
-    const float txv = F.ok ? __ldg(F.tx + xl) : 0.f;
-    unsigned yinm = 0;
-    float tyv[4];
+    unsigned yinm = 0, gzi = 0, gzo = 0;
 #pragma unroll
     for (int v = 0; v < 4; v++) {
         const int yy = min(y0 + v, (int)L.ny - 1);
-        yinm |= (unsigned)(yy >= zb.y0 && yy < zb.y1) << v;
-        tyv[v] = F.ok ? __ldg(F.ty + yy) : 0.f;
+        const bool yo = !(yy >= zb.y0 && yy < zb.y1), xo = !xin;
+        yinm |= (unsigned)!yo << v;
+        gzi |= (unsigned)((xo && yo) || ((xo != yo) && !F.ok)) << v;
+        gzo |= (unsigned)(xo || yo || !F.ok) << v;
     }
     const bool colin = xin && yinm == 15u;
+    const unsigned flags = yinm | (gzi << 4) | (gzo << 8) | ((unsigned)xin << 12);
 
-    // per-point operands of the next plane, fetched a plane ahead
-    V4 nprev, ncoef, ng = vzero();
-    float ntz = 0.f;
+    // per-point operands of the next plane, fetched a plane ahead (p: the
+    // plane's element offset of this thread's first point)
+    V4 nprev, ncoef, ngz = vzero();
     bool nbox = true;
-    unsigned nneed = 0;
-    auto fetch = [&](int zz) {
-        const long long p = (long long)zz * L.plane + offl;
+    auto fetch = [&](int zz, long long p) {
         nprev = ld_v4(up + p, true);
         ncoef = ldg_v4(coefC + p, true);
-        const bool zin = zz >= zb.z0 && zz < zb.z1;
-        nbox = zin && colin;
-        nneed = 0;
-        if (!nbox) {
-            ntz = F.ok ? __ldg(F.tz + zz) : 0.f;
-#pragma unroll
-            for (int v = 0; v < 4; v++) {
-                const int out = !zin + !xin + !((yinm >> v) & 1u);
-                nneed |= (unsigned)(out >= 2 || (!F.ok && out >= 1)) << v;
-            }
-            ng = ldg_v4(F.damp + p, nneed != 0);
-        }
+        if (GZ_R) ngz = ldg_v4(gz + p, true);
+        nbox = colin && zz >= zb.z0 && zz < zb.z1;
     };
-    fetch(zbeg);
+    long long zoff = (long long)zbeg * L.plane + offl;  // this plane's offset
+    fetch(zbeg, zoff);
     int aborted_at = -1;
-    long long zoff = (long long)zbeg * L.plane;
 
     auto plane_step = [&](const int z, const int J, const int m) -> bool {
         constexpr bool kStatic = QN % kTmStages == 0;
@@ -250,32 +275,30 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         const unsigned parity = kStatic ? (unsigned)(((QN / kTmStages) * m + J / kTmStages) & 1)
                                         : (unsigned)((it / kTmStages) & 1);
         auto slot = [&](int d) { return (J + R + d) % QN; };  // plane z + d
-        const bool zin = z >= zb.z0 && z < zb.z1;
-        const V4 vprev = nprev, vcoef = ncoef, vg = ng;
+        const V4 vprev = nprev, vcoef = ncoef, vgz = ngz;
         const bool inbox = nbox;
-        const unsigned need = nneed;
-        const float vtz = ntz;
 
-        unsigned ur[QC];
-        tmem_ld_cols<QC>(tu, ur);  // u ring (asynchronous)
+        unsigned ur[TM_U ? QC : 1];
+        if (TM_U) tmem_ld_cols<QC>(tu, ur);  // u ring (asynchronous)
         V4 hu = vzero(), hr = vzero();
         const bool more = z + 1 < zend;
-        if (more) {  // ring heads (plane z+R+1) and the next plane's operands
-            const long long ph = zoff + (long long)(R + 1) * L.plane + offl;
-            hu = ldg_v4(uc + ph, true);
-            if (VD) hr = ldg_v4(den + ph, true);
-            fetch(z + 1);
-        }
-        const long long pz = zoff + off;
+        const long long pz = zoff;
         zoff += L.plane;
+        if (more) {  // queue heads (plane z+R+1) and the next plane's operands
+            const long long ph = pz + (long long)(R + 1) * L.plane;
+            hu = ldg_v4(uc + ph, true);
+            if (TM_R || SM_R || RG_R) hr = ldg_v4(den + ph, true);
+            fetch(z + 1, zoff);
+        }
 
-        // z axis of u from the ring (c0 u first, then k = 1 .. R)
-        tmem_wait_ld<QC>(ur);
-        const V4 u0 = ring_at(ur, slot(0));
+        // z axis of u (c0 u first, then k = 1 .. R)
+        if (TM_U) tmem_wait_ld<QC>(ur);
+        auto uq = [&](int d) -> V4 { return TM_U ? ring_at(ur, slot(d)) : qu[slot(d)]; };
+        const V4 u0 = uq(0);
         V4 sdz = vmul(w2[0], u0), fuz = vzero();
 #pragma unroll
         for (int k = 1; k <= R; k++) {
-            const V4 a = ring_at(ur, slot(k)), b = ring_at(ur, slot(-k));
+            const V4 a = uq(k), b = uq(-k);
             sdz = vs(k, vadd(a, b), sdz);
             if (VD) fuz = vw(k == 1, k, vsub(a, b), fuz);
         }
@@ -323,8 +346,8 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             lap = vfma({PW.ih2[1]}, sdx, lap);
             lap = vfma({PW.ih2[0]}, sdz, lap);
             if (VD) {
-                unsigned rr[QC];
-                tmem_ld_cols<QC>(tr, rr);  // density ring (asynchronous)
+                unsigned rr[TM_R ? QC : 1];
+                if (TM_R) tmem_ld_cols<QC>(tr, rr);  // density ring (asynchronous)
                 V4 rho0, fry, frx = vzero();
                 {
                     P2 ev[2 * NC], od[2 * NC - 1];
@@ -348,15 +371,23 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                     const V4 b = lds_v4(trs - k * TW + HY);
                     frx = vw(k == 1, k, vsub(a, b), frx);
                 }
-                tmem_wait_ld<QC>(rr);
-                V4 frz = vzero();
-#pragma unroll
-                for (int k = 1; k <= R; k++)
-                    frz = vw(k == 1, k, vsub(ring_at(rr, slot(k)), ring_at(rr, slot(-k))), frz);
-                // cross = (fy gy / (4 hy^2) + fx gx / (4 hx^2) + fz gz / (4 hz^2))
+                // cross = fy gy / (4 hy^2) + fx gx / (4 hx^2) + fz gz / (4 hz^2)
                 V4 cross = vmul({PW.s1[2]}, {mul2(fuy.lo, fry.lo), mul2(fuy.hi, fry.hi)});
                 cross = vfma({PW.s1[1]}, {mul2(fux.lo, frx.lo), mul2(fux.hi, frx.hi)}, cross);
-                cross = vfma({PW.s1[0]}, {mul2(fuz.lo, frz.lo), mul2(fuz.hi, frz.hi)}, cross);
+                if (GZ_R) {
+                    cross = {fma2(fuz.lo, vgz.lo, cross.lo), fma2(fuz.hi, vgz.hi, cross.hi)};
+                } else {
+                    if (TM_R) tmem_wait_ld<QC>(rr);
+                    auto rq = [&](int d) -> V4 {
+                        if constexpr (TM_R) return ring_at(rr, slot(d));
+                        else if constexpr (RG_R) return qr[slot(d)];
+                        else return lds_v4(sq + slot(d) * NT);
+                    };
+                    V4 frz = vzero();
+#pragma unroll
+                    for (int k = 1; k <= R; k++) frz = vw(k == 1, k, vsub(rq(k), rq(-k)), frz);
+                    cross = vfma({PW.s1[0]}, {mul2(fuz.lo, frz.lo), mul2(fuz.hi, frz.hi)}, cross);
+                }
                 const float4 rr4 = to_f4(rho0);
                 const V4 inv = from_f4(make_float4(rcp_approx(rr4.x), rcp_approx(rr4.y),
                                                    rcp_approx(rr4.z), rcp_approx(rr4.w)));
@@ -370,13 +401,23 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                 const P2 m1{PW.minus_one};
                 a = {fma2(m1, vprev.lo, add2(u0.lo, u0.lo)), fma2(m1, vprev.hi, add2(u0.hi, u0.hi))};
             } else {
-                float d[4];
-                const float4 g4 = to_f4(vg);
+                const bool zin = z >= zb.z0 && z < zb.z1;
+                const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
+                const V4 gm = ldg_v4(F.damp + pz, need != 0);
+                const float4 g4 = to_f4(gm);
                 const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                const bool xin_ = (flags >> 12) & 1u;
+                const float tzv = (!zin && F.ok) ? __ldg(F.tz + z) : 0.f;
+                const float txv = (zin && !xin_ && F.ok) ? __ldg(F.tx + xl) : 0.f;
+                float d[4];
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
-                    const float face = (!zin ? vtz : 0.f) + (!xin ? txv : 0.f) +
-                                       (((yinm >> v) & 1u) ? 0.f : tyv[v]);
+                    const bool yo = !((flags >> v) & 1u);
+                    const float face =
+                        !zin ? tzv
+                             : (!xin_ ? txv
+                                      : ((yo && F.ok) ? __ldg(F.ty + min(y0 + v, (int)L.ny - 1))
+                                                      : 0.f));
                     d[v] = ((need >> v) & 1u) ? gg[v] : face;
                 }
                 const V4 dv = from_f4(make_float4(d[0], d[1], d[2], d[3]));
@@ -387,20 +428,24 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                      fma2(sub2(t.hi, one), vprev.hi, mul2(sub2(two, t.hi), u0.hi))};
             }
             const V4 out = {fma2(lap.lo, vcoef.lo, a.lo), fma2(lap.hi, vcoef.hi, a.hi)};
+            float* po = un + pz + dstore;
             if (full) {
-                *reinterpret_cast<ulonglong2*>(un + pz) = make_ulonglong2(out.lo.v, out.hi.v);
+                *reinterpret_cast<ulonglong2*>(po) = make_ulonglong2(out.lo.v, out.hi.v);
             } else if (any) {
                 const float4 o = to_f4(out);
                 const float ov[4] = {o.x, o.y, o.z, o.w};
 #pragma unroll
                 for (int v = 0; v < 4; v++)
-                    if (y0 + v < ylim) un[pz + v] = ov[v];
+                    if (y0 + v < ylim) po[v] = ov[v];
             }
         }
-        // ring heads into the slot plane z - R leaves
+        // queue heads into the slot plane z - R leaves
         if (more) {
-            tmem_st_v4(tu + 4 * slot(-R), hu);
-            if (VD) tmem_st_v4(tr + 4 * slot(-R), hr);
+            if (TM_U) tmem_st_v4(tu + 4 * slot(-R), hu);
+            else qu[slot(-R)] = hu;
+            if (TM_R) tmem_st_v4(tr + 4 * slot(-R), hr);
+            if (SM_R) sts_v4(sq + slot(-R) * NT, hr);
+            if (RG_R) qr[slot(-R)] = hr;
         }
         __syncthreads();  // the stage is free again; abort is uniform here
         if (s_abort) {
@@ -411,7 +456,7 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             issue(z + kTmStages, stage);
             issued++;
         }
-        tmem_wait_st();  // the next plane's ring loads see the heads
+        if (USE_TMEM) tmem_wait_st();  // the next plane's ring loads see the heads
         return true;
     };
 
@@ -428,12 +473,14 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         for (int p = aborted_at; p < issued; p++)
             mbar_wait(&bars[p % kTmStages], (unsigned)((p / kTmStages) & 1));
     }
-    // every warp is done with TMEM before the allocating warp frees it
-    tmem_wait_st();
-    tmem_fence_before_sync();
-    __syncthreads();
-    tmem_fence_after_sync();
-    if (warp == 0) tmem_dealloc(tbase, TT::NCOLS);
+    if (USE_TMEM) {
+        // every warp is done with TMEM before the allocating warp frees it
+        tmem_wait_st();
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+        if (warp == 0) tmem_dealloc(tbase, TT::NCOLS);
+    }
 }
 
 // ---- damping tables ------------------------------------------------------------
@@ -512,25 +559,27 @@ int tm_chunk(int ty, int tx, int nzi, int R, int per_sm) {
 }
 
 // Shared memory of a CTA: the tiles, padded so that no more than MINB CTAs
-// fit on an SM (their TMEM allocations must fit the SM's 512 columns).
-template <int R, bool VD, int XW, int MINB>
+// fit on an SM when they hold TMEM (their allocations must fit the SM's 512
+// columns).
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ>
 size_t tm_smem() {
-    using TT = TmTile<R, VD, XW>;
-    static_assert(MINB * TT::NCOLS <= 512, "TMEM columns of the resident CTAs");
+    using TT = TmTile<R, VD, XW, UQ, RZ>;
+    static_assert(TT::WC == 0 || MINB * TT::NCOLS <= 512, "TMEM columns of the resident CTAs");
+    if (TT::WC == 0) return TT::SMEM;
     const size_t per_sm = 228 * 1024;
     const size_t floor = per_sm / (MINB + 1) + 1024;
     return std::max(TT::SMEM, floor);
 }
 
-template <int R, bool VD, int XW, int MINB>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ>
 void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
                const float* den, const Layout& L, const Weights<float>& W,
                const TiledContext& ctx, cudaStream_t st) {
-    auto kernel = stencil3d_tmem<R, VD, XW, MINB>;
+    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ>;
     static std::atomic<bool> configured[64];
     int dev = 0;
     cudaGetDevice(&dev);
-    const size_t smem = tm_smem<R, VD, XW, MINB>();
+    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ>();
     if (!configured[dev & 63]) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[dev & 63] = true;
@@ -548,13 +597,63 @@ void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
     dim3 grid(ty, tx, zsplit);
     kernel<<<grid, 32 * XW, smem, st>>>(
         *reinterpret_cast<const CUtensorMap*>(ctx.map_u_tm),
-        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), un, uc, up, coefC, den, F, L, PW,
-        ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), un, uc, up, coefC, den,
+        ctx.coefGz, F, L, PW, ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
+}
+
+// Kernel configuration of the TMEM policies: u queue and density z term
+// (SIMWAVE_TM_VARIANT="uq,rz" overrides it for measurements).
+struct TmVariant {
+    int uq = 1, rz = 0;
+};
+TmVariant tm_variant() {
+    static TmVariant v = [] {
+        TmVariant t;
+        if (const char* e = std::getenv("SIMWAVE_TM_VARIANT")) {
+            int a = 1, b = 0;
+            if (std::sscanf(e, "%d,%d", &a, &b) == 2 && a >= 0 && a <= 1 && b >= 0 && b <= 3) {
+                t.uq = a;
+                t.rz = b;
+            }
+        }
+        return t;
+    }();
+    return v;
+}
+
+template <int R, bool VD, int XW, int MINB>
+void launch_tm_variant(float* un, const float* uc, const float* up, const float* coefC,
+                       const float* den, const Layout& L, const Weights<float>& W,
+                       const TiledContext& ctx, cudaStream_t st) {
+    const TmVariant v = tm_variant();
+    int rz = v.rz;
+    if (rz == 2 && !ctx.coefGz) rz = 1;
+    if (R != 4 || !VD) {
+        launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
+        return;
+    }
+    if (v.uq == 1) {
+        if (rz == 0) launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
+        else if (rz == 1) launch_tm<R, VD, XW, MINB, 1, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+        else if (rz == 2) launch_tm<R, VD, XW, MINB, 1, 2>(un, uc, up, coefC, den, L, W, ctx, st);
+        else launch_tm<R, VD, XW, MINB, 1, 3>(un, uc, up, coefC, den, L, W, ctx, st);
+    } else {
+        if (rz == 0) launch_tm<R, VD, XW, MINB, 0, 0>(un, uc, up, coefC, den, L, W, ctx, st);
+        else if (rz == 1) launch_tm<R, VD, XW, MINB, 0, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+        else if (rz == 2) launch_tm<R, VD, XW, MINB, 0, 2>(un, uc, up, coefC, den, L, W, ctx, st);
+        else launch_tm<R, VD, XW, MINB, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);
+    }
 }
 
 }  // namespace
 
-int tmem_rows(int policy) { return policy == SIMWAVE_POLICY_TMEM_WIDE ? 16 : 8; }
+int tmem_rows(int policy) {
+    if (policy != SIMWAVE_POLICY_TMEM_WIDE) return 8;
+    const char* e = std::getenv("SIMWAVE_TM_WIDE_ROWS");
+    return (e && std::atoi(e) == 12) ? 12 : 16;
+}
+
+bool tmem_wants_density_z() { return tm_variant().rz == 2; }
 
 void damp_face_tables(const float* damp, const Layout& L, const int* box, float* tz,
                       float* tx, float* ty, int* bad, cudaStream_t st) {
@@ -569,15 +668,22 @@ bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const 
                  const Weights<float>& W, cudaStream_t st) {
     if (!ctx.tm || L.r > 4 || !ctx.damp || !ctx.damp_tz) return false;
     const bool wide = policy == SIMWAVE_POLICY_TMEM_WIDE;
-    if (wide != (ctx.tm_rows == 16)) return false;
+    if (wide != (ctx.tm_rows != 8)) return false;
+    if (ctx.tm_rows == 12) {
+        if (vd && L.r == 4) {
+            launch_tm_variant<4, true, 12, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+            return true;
+        }
+        return false;
+    }
 #define SW_TM(RR)                                                                  \
     case RR:                                                                       \
         if (vd) {                                                                  \
-            if (wide) launch_tm<RR, true, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st);  \
-            else launch_tm<RR, true, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);        \
+            if (wide) launch_tm_variant<RR, true, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st);  \
+            else launch_tm_variant<RR, true, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);        \
         } else {                                                                   \
-            if (wide) launch_tm<RR, false, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st); \
-            else launch_tm<RR, false, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);       \
+            if (wide) launch_tm_variant<RR, false, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st); \
+            else launch_tm_variant<RR, false, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);       \
         }                                                                          \
         return true;
     switch (L.r) { SW_TM(1) SW_TM(2) SW_TM(3) SW_TM(4) }

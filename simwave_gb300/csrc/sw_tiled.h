@@ -123,6 +123,7 @@ int resolve_policy(int policy, int r, bool vd);
 // the launch, false when the context or the radius does not suit it (then
 // nothing is launched).
 int tmem_rows(int policy);
+bool tmem_wants_density_z();
 bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const float* uc,
                  const float* up, const float* coefC, const float* den, const Layout& L,
                  const Weights<float>& W, cudaStream_t st);
