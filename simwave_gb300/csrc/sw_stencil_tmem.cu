@@ -60,7 +60,7 @@ __host__ __device__ constexpr int pow2_at_least(int n) {
     return p;
 }
 
-template <int R, bool VD, int XW, int UQ = 1, int RZ = 0>
+template <int R, bool VD, int XW, int UQ = 1, int RZ = 0, int ST = kTmStages>
 struct TmTile {
     static constexpr int HY = round4(R);
     static constexpr int TW = 128 + 2 * HY;  // floats per tile row
@@ -75,8 +75,8 @@ struct TmTile {
     static constexpr int WC = (UQ == 1 ? QC : 0) + ((VD && RZ == 0) ? QC : 0);
     static constexpr int NCOLS = pow2_at_least((XW / 4) * WC);  // per CTA
     static constexpr int NF = VD ? 2 : 1;
-    static constexpr size_t SMEM = (size_t)NF * kTmStages * STRIDE * 4 +
-                                   ((VD && RZ == 1) ? (size_t)QN * 32 * XW * 16 : 0) + 64;
+    static constexpr size_t SMEM = (size_t)NF * ST * STRIDE * 4 +
+                                   ((VD && RZ == 1) ? (size_t)QN * 32 * XW * 16 : 0) + 256;
 };
 
 struct TmBox {  // interior box where the damping mask is zero
@@ -119,15 +119,17 @@ __device__ __forceinline__ V4 ring_at(const unsigned* r, int s) {
 //       shared memory, 2 the per-point array gz = s1_z sum_k c1_k (rho(z+k)
 //       - rho(z-k)) formed once per run (4 B more per point), 3 a queue in
 //       registers.
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM, int SY, int ST>
 __global__ void __launch_bounds__(32 * XW, MINB)
 stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                const __grid_constant__ CUtensorMap map_rho, float* un,
                const float* __restrict__ uc, const float* up,
                const float* __restrict__ coefC, const float* __restrict__ den,
-               const float* __restrict__ gz, TmDamp F, Layout L, PairWeights PW, float inv_dt,
+               const float* __restrict__ gz, const float* __restrict__ coefQ, TmDamp F, Layout L,
+               PairWeights PW, float inv_dt,
                int slot_cur, int zchunk, TmBox zb, int* __restrict__ err) {
-    using TT = TmTile<R, VD, XW, UQ, RZ>;
+    using TT = TmTile<R, VD, XW, UQ, RZ, ST>;
+    constexpr int S = ST;  // stages (planes in flight per field)
     constexpr int HY = TT::HY, TW = TT::TW, NC = TT::NC, QN = TT::QN, QC = TT::QC;
     constexpr int NF = TT::NF;
     constexpr int NT = 32 * XW;
@@ -138,12 +140,16 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     constexpr bool RG_R = VD && RZ == 3;
     constexpr bool USE_TMEM = TM_U || TM_R;
     float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [NF][stages][STRIDE]
-    float4* sq_base = reinterpret_cast<float4*>(tiles + NF * kTmStages * TT::STRIDE);
+    float4* sq_base = reinterpret_cast<float4*>(tiles + NF * S * TT::STRIDE);
     unsigned long long* bars =
         reinterpret_cast<unsigned long long*>(sq_base + (SM_R ? QN * NT : 0));
-    int* words = reinterpret_cast<int*>(bars + kTmStages);
+    int* words = reinterpret_cast<int*>(bars + S);
     int& s_abort = words[0];
     unsigned& s_tmem = *reinterpret_cast<unsigned*>(words + 1);
+    // stage release without a CTA barrier (SY): per stage, the count of warps
+    // that finished reading it and the plane index last loaded into it
+    unsigned* rel = reinterpret_cast<unsigned*>(words + 2);
+    int* last_it = words + 2 + S;
     if (smem_addr(tiles) & 127) {  // layout assumption broken: refuse
         if (threadIdx.x == 0) atomicExch(err, SIMWAVE_E_ARGUMENT);
         return;
@@ -176,7 +182,11 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     const int row0 = blockIdx.y * XW;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kTmStages; s++) mbar_init(&bars[s], 1);
+        for (int s = 0; s < S; s++) {
+            mbar_init(&bars[s], 1);
+            rel[s] = 0;
+            last_it[s] = -1;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
@@ -191,17 +201,16 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     const unsigned tr = tu + (TM_U ? QC : 0);
 
     auto issue = [&](int plane, int stage) {
+        last_it[stage] = plane - zbeg;
         mbar_expect_tx(&bars[stage], NF * TT::BYTES);
         tma_load_4d(tiles + stage * TT::STRIDE, &map_u, &bars[stage], col0, row0, plane,
                     slot_cur);
         if (VD)
-            tma_load_4d(tiles + (kTmStages + stage) * TT::STRIDE, &map_rho, &bars[stage], col0,
+            tma_load_4d(tiles + (S + stage) * TT::STRIDE, &map_rho, &bars[stage], col0,
                         row0, plane, 0);
     };
-    int issued = 0;
     if (threadIdx.x == 0)
-        for (; issued < kTmStages && zbeg + issued < zend; issued++)
-            issue(zbeg + issued, issued);
+        for (int i = 0; i < S && zbeg + i < zend; i++) issue(zbeg + i, i);
 
     P2 w2[R + 1], w1[R + 1];
 #pragma unroll
@@ -256,26 +265,31 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
 
     // per-point operands of the next plane, fetched a plane ahead (p: the
     // plane's element offset of this thread's first point)
-    V4 nprev, ncoef, ngz = vzero();
+    V4 nprev, ncoef, ngz = vzero(), nq = vzero();
     bool nbox = true;
     auto fetch = [&](int zz, long long p) {
         nprev = ld_v4(up + p, true);
         ncoef = ldg_v4(coefC + p, true);
         if (GZ_R) ngz = ldg_v4(gz + p, true);
         nbox = colin && zz >= zb.z0 && zz < zb.z1;
+        if (DM == 1) nq = ldg_v4(coefQ + p, !nbox);
     };
     long long zoff = (long long)zbeg * L.plane + offl;  // this plane's offset
     fetch(zbeg, zoff);
     int aborted_at = -1;
 
     auto plane_step = [&](const int z, const int J, const int m) -> bool {
-        constexpr bool kStatic = QN % kTmStages == 0;
+        constexpr bool kStatic = QN % S == 0;
         const int it = QN * m + J;
-        const int stage = kStatic ? J % kTmStages : it % kTmStages;
-        const unsigned parity = kStatic ? (unsigned)(((QN / kTmStages) * m + J / kTmStages) & 1)
-                                        : (unsigned)((it / kTmStages) & 1);
+        const int stage = kStatic ? J % S : it % S;
+        const unsigned parity = kStatic ? (unsigned)(((QN / S) * m + J / S) & 1)
+                                        : (unsigned)((it / S) & 1);
         auto slot = [&](int d) { return (J + R + d) % QN; };  // plane z + d
-        const V4 vprev = nprev, vcoef = ncoef, vgz = ngz;
+        if (SY && *(volatile int*)&s_abort) {  // another warp gave up
+            aborted_at = it;
+            return false;
+        }
+        const V4 vprev = nprev, vcoef = ncoef, vgz = ngz, vq = nq;
         const bool inbox = nbox;
 
         unsigned ur[TM_U ? QC : 1];
@@ -309,7 +323,7 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         if (ok) {
             const float* tus = tiles + stage * TT::STRIDE + (warp + R) * TW + 4 * lane;
             const float* trs =
-                tiles + (kTmStages + stage) * TT::STRIDE + (warp + R) * TW + 4 * lane;
+                tiles + (S + stage) * TT::STRIDE + (warp + R) * TW + 4 * lane;
             // y axis of u on pairs: even offsets straight from the 16-byte
             // loads, odd offsets repacked once
             V4 sdy, fuy;
@@ -397,10 +411,18 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             }
             // a = (2 - t) u - (1 - t) u_prev, t = damp C / dt (0 in the box)
             V4 a;
-            if (inbox) {
-                const P2 m1{PW.minus_one};
-                a = {fma2(m1, vprev.lo, add2(u0.lo, u0.lo)), fma2(m1, vprev.hi, add2(u0.hi, u0.hi))};
-            } else {
+            if (DM == 1) {
+                // with Q: a = 2 u - (1 - q) u_prev, divided by 1 + q off the box
+                const P2 one{PW.one};
+                a = {fma2(sub2(vq.lo, one), vprev.lo, add2(u0.lo, u0.lo)),
+                     fma2(sub2(vq.hi, one), vprev.hi, add2(u0.hi, u0.hi))};
+                if (!inbox) {
+                    const float4 qq = to_f4(vq);
+                    const V4 rq = from_f4(make_float4(rcp_approx(1.f + qq.x), rcp_approx(1.f + qq.y),
+                                                      rcp_approx(1.f + qq.z), rcp_approx(1.f + qq.w)));
+                    a = {mul2(a.lo, rq.lo), mul2(a.hi, rq.hi)};
+                }
+            } else if (inbox) {            } else {
                 const bool zin = z >= zb.z0 && z < zb.z1;
                 const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
                 const V4 gm = ldg_v4(F.damp + pz, need != 0);
@@ -447,14 +469,32 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             if (SM_R) sts_v4(sq + slot(-R) * NT, hr);
             if (RG_R) qr[slot(-R)] = hr;
         }
-        __syncthreads();  // the stage is free again; abort is uniform here
-        if (s_abort) {
-            aborted_at = it;
-            return false;
-        }
-        if (threadIdx.x == 0 && z + kTmStages < zend) {
-            issue(z + kTmStages, stage);
-            issued++;
+        if (SY) {
+            // the warp is done with the stage: the last warp to finish it
+            // loads plane z + S into it
+            __syncwarp();
+            if (!ok) {
+                aborted_at = it;
+                return false;
+            }
+            if (lane == 0) {
+                unsigned old;
+                asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;"
+                             : "=r"(old)
+                             : "r"(smem_addr(&rel[stage]))
+                             : "memory");
+                if ((old + 1) % XW == 0 && z + S < zend) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(z + S, stage);
+                }
+            }
+        } else {
+            __syncthreads();  // the stage is free again; abort is uniform here
+            if (s_abort) {
+                aborted_at = it;
+                return false;
+            }
+            if (threadIdx.x == 0 && z + S < zend) issue(z + S, stage);
         }
         if (USE_TMEM) tmem_wait_st();  // the next plane's ring loads see the heads
         return true;
@@ -468,10 +508,12 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         }
         if (aborted_at >= 0) break;
     }
-    if (aborted_at >= 0 && threadIdx.x == 0) {
+    if (SY) __syncthreads();  // every warp has left the plane loop
+    if (threadIdx.x == 0 && (s_abort || aborted_at >= 0)) {
         atomicExch(err, SIMWAVE_E_TIMEOUT);
-        for (int p = aborted_at; p < issued; p++)
-            mbar_wait(&bars[p % kTmStages], (unsigned)((p / kTmStages) & 1));
+        // drain the copies still in flight into this CTA's shared memory
+        for (int s = 0; s < S; s++)
+            if (last_it[s] >= 0) mbar_wait(&bars[s], (unsigned)((last_it[s] / S) & 1));
     }
     if (USE_TMEM) {
         // every warp is done with TMEM before the allocating warp frees it
@@ -561,9 +603,9 @@ int tm_chunk(int ty, int tx, int nzi, int R, int per_sm) {
 // Shared memory of a CTA: the tiles, padded so that no more than MINB CTAs
 // fit on an SM when they hold TMEM (their allocations must fit the SM's 512
 // columns).
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int ST>
 size_t tm_smem() {
-    using TT = TmTile<R, VD, XW, UQ, RZ>;
+    using TT = TmTile<R, VD, XW, UQ, RZ, ST>;
     static_assert(TT::WC == 0 || MINB * TT::NCOLS <= 512, "TMEM columns of the resident CTAs");
     if (TT::WC == 0) return TT::SMEM;
     const size_t per_sm = 228 * 1024;
@@ -571,15 +613,16 @@ size_t tm_smem() {
     return std::max(TT::SMEM, floor);
 }
 
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM = 0, int SY = 0,
+          int ST = kTmStages>
 void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
                const float* den, const Layout& L, const Weights<float>& W,
                const TiledContext& ctx, cudaStream_t st) {
-    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ>;
+    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ, DM, SY, ST>;
     static std::atomic<bool> configured[64];
     int dev = 0;
     cudaGetDevice(&dev);
-    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ>();
+    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ, ST>();
     if (!configured[dev & 63]) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[dev & 63] = true;
@@ -598,27 +641,43 @@ void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
     kernel<<<grid, 32 * XW, smem, st>>>(
         *reinterpret_cast<const CUtensorMap*>(ctx.map_u_tm),
         *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), un, uc, up, coefC, den,
-        ctx.coefGz, F, L, PW, ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
+        ctx.coefGz, ctx.coefQ, F, L, PW, ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
 }
 
-// Kernel configuration of the TMEM policies: u queue and density z term
-// (SIMWAVE_TM_VARIANT="uq,rz" overrides it for measurements).
+// Kernel configuration of the TMEM policies: u queue, density z term,
+// damping source, stage release and stage count
+// (SIMWAVE_TM_VARIANT="uq,rz,dm,sy,st" overrides it for measurements).
 struct TmVariant {
-    int uq = 1, rz = 0;
+    int uq = 1, rz = 0, dm = 0, sy = 0, st = 3;
 };
 TmVariant tm_variant() {
     static TmVariant v = [] {
         TmVariant t;
         if (const char* e = std::getenv("SIMWAVE_TM_VARIANT")) {
-            int a = 1, b = 0;
-            if (std::sscanf(e, "%d,%d", &a, &b) == 2 && a >= 0 && a <= 1 && b >= 0 && b <= 3) {
+            int a = 1, b = 0, c = 0, d = 0, f = 3;
+            const int n = std::sscanf(e, "%d,%d,%d,%d,%d", &a, &b, &c, &d, &f);
+            if (n >= 2 && a >= 0 && a <= 1 && b >= 0 && b <= 3 && c >= 0 && c <= 1 &&
+                d >= 0 && d <= 1 && (f == 3 || f == 4 || f == 6)) {
                 t.uq = a;
                 t.rz = b;
+                t.dm = c;
+                t.sy = d;
+                t.st = f;
             }
         }
         return t;
     }();
     return v;
+}
+
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM>
+void launch_tm_sync(int sy, int stg, float* un, const float* uc, const float* up,
+                    const float* coefC, const float* den, const Layout& L,
+                    const Weights<float>& W, const TiledContext& ctx, cudaStream_t st) {
+    if (!sy) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);
+    if (stg == 4) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 4>(un, uc, up, coefC, den, L, W, ctx, st);
+    if (stg == 6) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 6>(un, uc, up, coefC, den, L, W, ctx, st);
+    launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 3>(un, uc, up, coefC, den, L, W, ctx, st);
 }
 
 template <int R, bool VD, int XW, int MINB>
@@ -632,17 +691,17 @@ void launch_tm_variant(float* un, const float* uc, const float* up, const float*
         launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
         return;
     }
-    if (v.uq == 1) {
-        if (rz == 0) launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
-        else if (rz == 1) launch_tm<R, VD, XW, MINB, 1, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-        else if (rz == 2) launch_tm<R, VD, XW, MINB, 1, 2>(un, uc, up, coefC, den, L, W, ctx, st);
-        else launch_tm<R, VD, XW, MINB, 1, 3>(un, uc, up, coefC, den, L, W, ctx, st);
-    } else {
-        if (rz == 0) launch_tm<R, VD, XW, MINB, 0, 0>(un, uc, up, coefC, den, L, W, ctx, st);
-        else if (rz == 1) launch_tm<R, VD, XW, MINB, 0, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-        else if (rz == 2) launch_tm<R, VD, XW, MINB, 0, 2>(un, uc, up, coefC, den, L, W, ctx, st);
-        else launch_tm<R, VD, XW, MINB, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);
+#define SW_TMV(UQV, RZV)                                                                    \
+    if (v.uq == UQV && rz == RZV) {                                                         \
+        if (v.dm) launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 1>(v.sy, v.st, un, uc, up, coefC, \
+                                                              den, L, W, ctx, st);          \
+        else launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 0>(v.sy, v.st, un, uc, up, coefC,     \
+                                                         den, L, W, ctx, st);               \
+        return;                                                                             \
     }
+    SW_TMV(1, 0) SW_TMV(1, 2) SW_TMV(0, 2) SW_TMV(0, 1)
+#undef SW_TMV
+    launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
 }
 
 }  // namespace
