@@ -422,7 +422,10 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                                                       rcp_approx(1.f + qq.z), rcp_approx(1.f + qq.w)));
                     a = {mul2(a.lo, rq.lo), mul2(a.hi, rq.hi)};
                 }
-            } else if (inbox) {            } else {
+            } else if (inbox) {
+                const P2 m1{PW.minus_one};
+                a = {fma2(m1, vprev.lo, add2(u0.lo, u0.lo)), fma2(m1, vprev.hi, add2(u0.hi, u0.hi))};
+            } else {
                 const bool zin = z >= zb.z0 && z < zb.z1;
                 const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
                 const V4 gm = ldg_v4(F.damp + pz, need != 0);
