@@ -262,10 +262,21 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     }
     const bool colin = xin && yinm == 15u;
     const unsigned flags = yinm | (gzi << 4) | (gzo << 8) | ((unsigned)xin << 12);
+    // DM 2: the thread's face values with z inside the box, held in registers
+    float dzi[4] = {0.f, 0.f, 0.f, 0.f};
+    if (DM == 2 && F.ok) {
+        const float txv = __ldg(F.tx + xl);
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const bool yo = !((yinm >> v) & 1u);
+            if (yo != !xin) dzi[v] = !xin ? txv : __ldg(F.ty + min(y0 + v, (int)L.ny - 1));
+        }
+    }
 
     // per-point operands of the next plane, fetched a plane ahead (p: the
     // plane's element offset of this thread's first point)
-    V4 nprev, ncoef, ngz = vzero(), nq = vzero();
+    V4 nprev, ncoef, ngz = vzero(), nq = vzero(), ng = vzero();
+    float ntz = 0.f;
     bool nbox = true;
     auto fetch = [&](int zz, long long p) {
         nprev = ld_v4(up + p, true);
@@ -273,6 +284,12 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         if (GZ_R) ngz = ldg_v4(gz + p, true);
         nbox = colin && zz >= zb.z0 && zz < zb.z1;
         if (DM == 1) nq = ldg_v4(coefQ + p, !nbox);
+        if (DM == 2 && !nbox) {  // the z table and the mask of the next plane
+            const bool zin = zz >= zb.z0 && zz < zb.z1;
+            const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
+            ntz = (!zin && F.ok) ? __ldg(F.tz + zz) : 0.f;
+            ng = ldg_v4(F.damp + p, need != 0);
+        }
     };
     long long zoff = (long long)zbeg * L.plane + offl;  // this plane's offset
     fetch(zbeg, zoff);
@@ -289,7 +306,8 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             aborted_at = it;
             return false;
         }
-        const V4 vprev = nprev, vcoef = ncoef, vgz = ngz, vq = nq;
+        const V4 vprev = nprev, vcoef = ncoef, vgz = ngz, vq = nq, vg = ng;
+        const float vtz = ntz;
         const bool inbox = nbox;
 
         unsigned ur[TM_U ? QC : 1];
@@ -422,6 +440,21 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                                                       rcp_approx(1.f + qq.z), rcp_approx(1.f + qq.w)));
                     a = {mul2(a.lo, rq.lo), mul2(a.hi, rq.hi)};
                 }
+            } else if (DM == 2 && !inbox) {
+                const bool zin = z >= zb.z0 && z < zb.z1;
+                const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
+                const float4 g4 = to_f4(vg);
+                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                float d[4];
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    d[v] = ((need >> v) & 1u) ? gg[v] : (zin ? dzi[v] : vtz);
+                const V4 dv = from_f4(make_float4(d[0], d[1], d[2], d[3]));
+                const P2 idt = pk(inv_dt, inv_dt);
+                const V4 t = {mul2(mul2(dv.lo, vcoef.lo), idt), mul2(mul2(dv.hi, vcoef.hi), idt)};
+                const P2 one{PW.one}, two{PW.two};
+                a = {fma2(sub2(t.lo, one), vprev.lo, mul2(sub2(two, t.lo), u0.lo)),
+                     fma2(sub2(t.hi, one), vprev.hi, mul2(sub2(two, t.hi), u0.hi))};
             } else if (inbox) {
                 const P2 m1{PW.minus_one};
                 a = {fma2(m1, vprev.lo, add2(u0.lo, u0.lo)), fma2(m1, vprev.hi, add2(u0.hi, u0.hi))};
@@ -659,7 +692,7 @@ TmVariant tm_variant() {
         if (const char* e = std::getenv("SIMWAVE_TM_VARIANT")) {
             int a = 1, b = 0, c = 0, d = 0, f = 3;
             const int n = std::sscanf(e, "%d,%d,%d,%d,%d", &a, &b, &c, &d, &f);
-            if (n >= 2 && a >= 0 && a <= 1 && b >= 0 && b <= 3 && c >= 0 && c <= 1 &&
+            if (n >= 2 && a >= 0 && a <= 1 && b >= 0 && b <= 3 && c >= 0 && c <= 2 &&
                 d >= 0 && d <= 1 && (f == 3 || f == 4 || f == 6)) {
                 t.uq = a;
                 t.rz = b;
@@ -678,9 +711,8 @@ void launch_tm_sync(int sy, int stg, float* un, const float* uc, const float* up
                     const float* coefC, const float* den, const Layout& L,
                     const Weights<float>& W, const TiledContext& ctx, cudaStream_t st) {
     if (!sy) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);
-    if (stg == 4) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 4>(un, uc, up, coefC, den, L, W, ctx, st);
     if (stg == 6) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 6>(un, uc, up, coefC, den, L, W, ctx, st);
-    launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 3>(un, uc, up, coefC, den, L, W, ctx, st);
+    launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 4>(un, uc, up, coefC, den, L, W, ctx, st);
 }
 
 template <int R, bool VD, int XW, int MINB>
@@ -690,19 +722,19 @@ void launch_tm_variant(float* un, const float* uc, const float* up, const float*
     const TmVariant v = tm_variant();
     int rz = v.rz;
     if (rz == 2 && !ctx.coefGz) rz = 1;
-    if (R != 4 || !VD) {
+    if (R != 4 || !VD || XW != 12) {
         launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
         return;
     }
 #define SW_TMV(UQV, RZV)                                                                    \
     if (v.uq == UQV && rz == RZV) {                                                         \
-        if (v.dm) launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 1>(v.sy, v.st, un, uc, up, coefC, \
-                                                              den, L, W, ctx, st);          \
-        else launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 0>(v.sy, v.st, un, uc, up, coefC,     \
-                                                         den, L, W, ctx, st);               \
+        if (v.dm == 1) launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 1>(v.sy, v.st, un, uc, up,  \
+                                                                   coefC, den, L, W, ctx, st); \
+        else launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 2>(v.sy, v.st, un, uc,                \
+                                                         up, coefC, den, L, W, ctx, st);     \
         return;                                                                             \
     }
-    SW_TMV(1, 0) SW_TMV(1, 2) SW_TMV(0, 2) SW_TMV(0, 1)
+    SW_TMV(0, 3) SW_TMV(0, 2) SW_TMV(0, 1) SW_TMV(0, 0)
 #undef SW_TMV
     launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
 }
