@@ -8,13 +8,13 @@ host when the shot completes.
 * 2D float32 shots join a running ``BatchEngine``: every epoch advances all
   admitted 2D shots by ``epoch_steps`` time steps in one graph-captured
   sequence, and newly admitted shots join at the next epoch.
-* Other shots (3D, or float64) run through the device entry on their own
-  stream, shortest first (interior updates), at most ``inflight`` queued at a
-  time, and only while no 2D shot is in the batch: each such shot fills the
-  GPU on its own, and its long-running blocks would hold every SM between the
-  batch's short launches (stream priority only orders blocks not yet
-  placed), delaying every 2D step; the batch, whose shots are the shorter
-  jobs, goes first.
+* Other shots (3D, or float64) run through the device entry, each on a
+  low-priority stream of its own, shortest first (interior updates), up to
+  ``inflight`` at a time, while the 2D batch keeps stepping on its
+  high-priority stream: their blocks fill the SMs the batch's short launches
+  leave idle (between epochs the host waits for the batch), and the block
+  scheduler places the batch's blocks first as SMs free up. With
+  ``overlap=False`` they wait until no 2D shot is in the batch instead.
 
 Latency of a request = completion time - arrival time (queueing, upload,
 compute and shot-record download included).
@@ -74,8 +74,8 @@ class Request:
 class ShotServer:
     """Serve requests with continuous batching on one GPU."""
 
-    def __init__(self, hbm_budget=None, epoch_steps=64, inflight=2, device="cuda",
-                 tile_rows=None, reserve_bytes=0, stage_workers=2, tuning=None):
+    def __init__(self, hbm_budget=None, epoch_steps=64, inflight=3, device="cuda",
+                 tile_rows=None, reserve_bytes=0, stage_workers=2, tuning=None, overlap=True):
         self.device = torch.device(device)
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
@@ -89,7 +89,11 @@ class ShotServer:
             self.engine.apply(tuning)
         lo, hi = torch.cuda.Stream.priority_range()
         self.epoch_stream = torch.cuda.Stream(self.device, priority=hi)
-        self.shot_stream = torch.cuda.Stream(self.device, priority=lo)
+        self.inflight = max(int(inflight), 1)
+        self.overlap = bool(overlap)
+        # one stream per stream-run shot in flight
+        self.shot_streams = [torch.cuda.Stream(self.device, priority=lo)
+                             for _ in range(self.inflight)]
         # uploads of stream-run shots happen on a worker thread and stream
         # so the serving loop keeps stepping the batch meanwhile
         self.stage_stream = torch.cuda.Stream(self.device)
@@ -100,12 +104,11 @@ class ShotServer:
             # carves problems out of it instead of calling cudaMalloc
             with torch.cuda.stream(self.stage_stream):
                 torch.empty(int(reserve_bytes), dtype=torch.uint8, device=self.device)
-        self.inflight = max(int(inflight), 1)
         self.pending = collections.deque()
         self.staging = []    # admitted requests whose device copies are being made
         self.active2d = {}   # shot id -> request
         self.ready = []      # admitted stream-run shots not yet launched
-        self.active = []     # (request, event) of launched stream-run shots
+        self.active = []     # (request, event, stream) of launched stream-run shots
         self.done = []
 
     # -- admission ----------------------------------------------------------
@@ -175,19 +178,22 @@ class ShotServer:
         return prob, ev
 
     def _launch(self):
-        """Queue the shortest admitted stream-run shots on the shot stream
-        (none while the 2D batch has shots or is about to get some)."""
+        """Queue the shortest admitted stream-run shots, each on a free shot
+        stream (with ``overlap=False``, none while the 2D batch has shots or
+        is about to get some)."""
         busy2d = bool(self.active2d) or any(r.batchable for r in self.staging)
-        while self.ready and len(self.active) < self.inflight and not busy2d:
+        while self.ready and len(self.active) < self.inflight and (self.overlap or not busy2d):
             req = min(self.ready, key=lambda r: r.updates)
             self.ready.remove(req)
-            self.shot_stream.wait_event(req._uploaded)
+            used = {id(s) for _, _, s in self.active}
+            stream = next(s for s in self.shot_streams if id(s) not in used)
+            stream.wait_event(req._uploaded)
             req._uploaded = None
             req.started = time.perf_counter()
-            req.problem.run(self.shot_stream)
+            req.problem.run(stream)
             ev = torch.cuda.Event()
-            ev.record(self.shot_stream)
-            self.active.append((req, ev))
+            ev.record(stream)
+            self.active.append((req, ev, stream))
 
     def _evict(self, need):
         for req in self.done:
@@ -218,12 +224,12 @@ class ShotServer:
                 self.engine.release(sid)
                 self._complete(self.active2d.pop(sid))
         still = []
-        for req, ev in self.active:
+        for req, ev, stream in self.active:
             if ev.query():
-                req.problem.status()
+                req.problem.status(stream)
                 self._complete(req)
             else:
-                still.append((req, ev))
+                still.append((req, ev, stream))
         self.active = still
         self._launch()
 

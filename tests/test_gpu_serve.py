@@ -89,3 +89,32 @@ def test_stream_shots_run_shortest_first():
     server.close()
     order = [r.tag for r in sorted(reqs, key=lambda r: r.completed)]
     assert order == [r.tag for r in sorted(reqs, key=lambda r: r.updates)]
+
+
+def test_3d_shots_overlap_2d_epochs_and_each_other():
+    """3D shots run while the 2D batch is stepping and several at once, and
+    every result equals the shot run alone."""
+    from simwave_gb300.serve import Request, ShotServer
+    reqs = []
+    for i in range(4):  # 2D shots long enough to keep the batch busy
+        kw = random_problem(sw, 2, 8, bool(i % 2), "none", 0, shape=(300, 420),
+                            tf=0.4, seed=200 + i, nrec=6)
+        reqs.append(Request(kw, 0.0, tag="2d%d" % i))
+    for i in range(3):
+        kw = random_problem(sw, 3, 8, i == 1, "none", 0, shape=(40, 44, 44),
+                            tf=0.08, seed=300 + i, nrec=5)
+        reqs.append(Request(kw, 0.0, tag="3d%d" % i))
+    server = ShotServer(epoch_steps=16, inflight=3)
+    server.prepare(reqs)
+    server.serve(reqs, timeout=300)
+    server.close()
+    two = [r for r in reqs if r.kind == "2d"]
+    three = [r for r in reqs if r.kind == "3d"]
+    last2d = max(r.completed for r in two)
+    assert any(r.started < last2d for r in three), "no 3D shot ran beside the 2D batch"
+    assert any(a.started < b.completed and b.started < a.completed
+               for a in three for b in three if a is not b), "3D shots ran one at a time"
+    for r in reqs:
+        u, rec = _alone(r.kwargs)
+        assert rel_l2(r.problem.u_full_numpy(), u) <= 1e-5, r.tag
+        assert rel_l2(r.shot_record, rec) <= 1e-5, r.tag
