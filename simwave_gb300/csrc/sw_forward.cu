@@ -357,6 +357,7 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         }
         ctx.coefC = C;
         ctx.coefQ = Q;
+        if (tm) tmem_encode_interior(ctx, L, (long long)R.nslots);
         ctx.err = device_words() + 7;
         ctx.ok = true;
     }

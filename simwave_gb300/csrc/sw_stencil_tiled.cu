@@ -1258,6 +1258,21 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
     return true;
 }
 
+void tmem_encode_interior(TiledContext& ctx, const Layout& L, long long nslots) {
+    ctx.tm_ti = false;
+    if (!ctx.tm || !ctx.coefC || !ctx.coefQ || !tmem_wants_interior()) return;
+    const int rows = ctx.tm_rows;
+    CUtensorMap mu, mc, mq;
+    if (encode_map(&mu, ctx.u_base, L, nslots, ctx.slot_stride, 128, rows) &&
+        encode_map(&mc, ctx.coefC, L, 1, L.nz * L.plane, 128, rows) &&
+        encode_map(&mq, ctx.coefQ, L, 1, L.nz * L.plane, 128, rows)) {
+        std::memcpy(ctx.map_up_tm, &mu, sizeof(mu));
+        std::memcpy(ctx.map_c_tm, &mc, sizeof(mc));
+        std::memcpy(ctx.map_q_tm, &mq, sizeof(mq));
+        ctx.tm_ti = true;
+    }
+}
+
 int resolve_policy(int policy, int r, bool vd) {
     return policy == SIMWAVE_POLICY_AUTO ? auto_policy(r, vd) : policy;
 }

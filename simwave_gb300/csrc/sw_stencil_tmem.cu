@@ -42,6 +42,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 
 #include "simwave_gb300.h"
 #include "sw_pairs.cuh"
@@ -60,7 +61,7 @@ __host__ __device__ constexpr int pow2_at_least(int n) {
     return p;
 }
 
-template <int R, bool VD, int XW, int UQ = 1, int RZ = 0, int ST = kTmStages>
+template <int R, bool VD, int XW, int UQ = 1, int RZ = 0, int ST = kTmStages, int TI = 0>
 struct TmTile {
     static constexpr int HY = round4(R);
     static constexpr int TW = 128 + 2 * HY;  // floats per tile row
@@ -75,8 +76,19 @@ struct TmTile {
     static constexpr int WC = (UQ == 1 ? QC : 0) + ((VD && RZ == 0) ? QC : 0);
     static constexpr int NCOLS = pow2_at_least((XW / 4) * WC);  // per CTA
     static constexpr int NF = VD ? 2 : 1;
-    static constexpr size_t SMEM = (size_t)NF * ST * STRIDE * 4 +
+    // TI: the per-point operands (u_prev, C, Q) of a plane arrive by TMA
+    // too, as 128 x XW boxes in the plane's stage
+    static constexpr int IN = 128 * XW;                       // floats of one box
+    static constexpr int SF = NF * STRIDE + (TI ? 3 * IN : 0);  // floats per stage
+    static constexpr size_t SMEM = (size_t)ST * SF * 4 +
                                    ((VD && RZ == 1) ? (size_t)QN * 32 * XW * 16 : 0) + 256;
+};
+
+// Boxes of the per-point operands (kernel parameter of the TI kernels).
+struct TmInterior {
+    CUtensorMap up;  // the wavefield slots (4D: pitched row, x, z, slot)
+    CUtensorMap c;   // C
+    CUtensorMap q;   // Q
 };
 
 struct TmBox {  // interior box where the damping mask is zero
@@ -119,16 +131,18 @@ __device__ __forceinline__ V4 ring_at(const unsigned* r, int s) {
 //       shared memory, 2 the per-point array gz = s1_z sum_k c1_k (rho(z+k)
 //       - rho(z-k)) formed once per run (4 B more per point), 3 a queue in
 //       registers.
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM, int SY, int ST>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM, int SY, int ST, int TI>
 __global__ void __launch_bounds__(32 * XW, MINB)
 stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
-               const __grid_constant__ CUtensorMap map_rho, float* un,
+               const __grid_constant__ CUtensorMap map_rho,
+               const __grid_constant__ TmInterior maps_in, float* un,
                const float* __restrict__ uc, const float* up,
                const float* __restrict__ coefC, const float* __restrict__ den,
                const float* __restrict__ gz, const float* __restrict__ coefQ, TmDamp F, Layout L,
                PairWeights PW, float inv_dt,
-               int slot_cur, int zchunk, TmBox zb, int* __restrict__ err) {
-    using TT = TmTile<R, VD, XW, UQ, RZ, ST>;
+               int slot_cur, int slot_prev, int zchunk, TmBox zb, int* __restrict__ err) {
+    using TT = TmTile<R, VD, XW, UQ, RZ, ST, TI>;
+    static_assert(!TI || DM == 1, "TMA-staged operands carry Q, not the damping tables");
     constexpr int S = ST;  // stages (planes in flight per field)
     constexpr int HY = TT::HY, TW = TT::TW, NC = TT::NC, QN = TT::QN, QC = TT::QC;
     constexpr int NF = TT::NF;
@@ -139,8 +153,9 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     constexpr bool GZ_R = VD && RZ == 2;
     constexpr bool RG_R = VD && RZ == 3;
     constexpr bool USE_TMEM = TM_U || TM_R;
-    float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [NF][stages][STRIDE]
-    float4* sq_base = reinterpret_cast<float4*>(tiles + NF * S * TT::STRIDE);
+    // stages: u tile, density tile, then (TI) the u_prev, C and Q boxes
+    float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [stages][SF]
+    float4* sq_base = reinterpret_cast<float4*>(tiles + S * TT::SF);
     unsigned long long* bars =
         reinterpret_cast<unsigned long long*>(sq_base + (SM_R ? QN * NT : 0));
     int* words = reinterpret_cast<int*>(bars + S);
@@ -200,14 +215,25 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         tbase + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)((warp >> 2) * TT::WC);
     const unsigned tr = tu + (TM_U ? QC : 0);
 
+    // TI: the CTA's whole tile lies in the zero box on plane p (no Q box)
+    const bool tile_xy_in = (R + blockIdx.y * XW >= zb.x0) && (R + (blockIdx.y + 1) * XW <= zb.x1) &&
+                            (yb >= zb.y0) && (yb + 128 <= zb.y1);
+    auto tile_in_box = [&](int p) { return tile_xy_in && p >= zb.z0 && p < zb.z1; };
     auto issue = [&](int plane, int stage) {
         last_it[stage] = plane - zbeg;
-        mbar_expect_tx(&bars[stage], NF * TT::BYTES);
-        tma_load_4d(tiles + stage * TT::STRIDE, &map_u, &bars[stage], col0, row0, plane,
-                    slot_cur);
-        if (VD)
-            tma_load_4d(tiles + (S + stage) * TT::STRIDE, &map_rho, &bars[stage], col0,
-                        row0, plane, 0);
+        float* sb = tiles + stage * TT::SF;
+        const bool q = TI && !tile_in_box(plane);
+        mbar_expect_tx(&bars[stage],
+                       NF * TT::BYTES + (TI ? (2 + (q ? 1 : 0)) * TT::IN * 4 : 0));
+        tma_load_4d(sb, &map_u, &bars[stage], col0, row0, plane, slot_cur);
+        if (VD) tma_load_4d(sb + TT::STRIDE, &map_rho, &bars[stage], col0, row0, plane, 0);
+        if (TI) {
+            float* si = sb + NF * TT::STRIDE;
+            const int ci = (int)L.lead + yb, ri = R + blockIdx.y * XW;
+            tma_load_4d(si, &maps_in.up, &bars[stage], ci, ri, plane, slot_prev);
+            tma_load_4d(si + TT::IN, &maps_in.c, &bars[stage], ci, ri, plane, 0);
+            if (q) tma_load_4d(si + 2 * TT::IN, &maps_in.q, &bars[stage], ci, ri, plane, 0);
+        }
     };
     if (threadIdx.x == 0)
         for (int i = 0; i < S && zbeg + i < zend; i++) issue(zbeg + i, i);
@@ -279,11 +305,13 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     float ntz = 0.f;
     bool nbox = true;
     auto fetch = [&](int zz, long long p) {
-        nprev = ld_v4(up + p, true);
-        ncoef = ldg_v4(coefC + p, true);
+        if (!TI) {
+            nprev = ld_v4(up + p, true);
+            ncoef = ldg_v4(coefC + p, true);
+        }
         if (GZ_R) ngz = ldg_v4(gz + p, true);
         nbox = colin && zz >= zb.z0 && zz < zb.z1;
-        if (DM == 1) nq = ldg_v4(coefQ + p, !nbox);
+        if (DM == 1 && !TI) nq = ldg_v4(coefQ + p, !nbox);
         if (DM == 2 && !nbox) {  // the z table and the mask of the next plane
             const bool zin = zz >= zb.z0 && zz < zb.z1;
             const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
@@ -306,7 +334,8 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             aborted_at = it;
             return false;
         }
-        const V4 vprev = nprev, vcoef = ncoef, vgz = ngz, vq = nq, vg = ng;
+        V4 vprev = nprev, vcoef = ncoef, vq = nq;
+        const V4 vgz = ngz, vg = ng;
         const float vtz = ntz;
         const bool inbox = nbox;
 
@@ -339,9 +368,15 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[stage], parity));
         if (!ok) s_abort = 1;
         if (ok) {
-            const float* tus = tiles + stage * TT::STRIDE + (warp + R) * TW + 4 * lane;
-            const float* trs =
-                tiles + (S + stage) * TT::STRIDE + (warp + R) * TW + 4 * lane;
+            const float* sb = tiles + stage * TT::SF;
+            const float* tus = sb + (warp + R) * TW + 4 * lane;
+            const float* trs = sb + TT::STRIDE + (warp + R) * TW + 4 * lane;
+            if (TI) {  // this plane's operands from its stage
+                const float* si = sb + NF * TT::STRIDE + warp * 128 + 4 * lane;
+                vprev = lds_v4(si);
+                vcoef = lds_v4(si + TT::IN);
+                if (!inbox) vq = lds_v4(si + 2 * TT::IN);
+            }
             // y axis of u on pairs: even offsets straight from the 16-byte
             // loads, odd offsets repacked once
             V4 sdy, fuy;
@@ -639,9 +674,9 @@ int tm_chunk(int ty, int tx, int nzi, int R, int per_sm) {
 // Shared memory of a CTA: the tiles, padded so that no more than MINB CTAs
 // fit on an SM when they hold TMEM (their allocations must fit the SM's 512
 // columns).
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int ST>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int ST, int TI>
 size_t tm_smem() {
-    using TT = TmTile<R, VD, XW, UQ, RZ, ST>;
+    using TT = TmTile<R, VD, XW, UQ, RZ, ST, TI>;
     static_assert(TT::WC == 0 || MINB * TT::NCOLS <= 512, "TMEM columns of the resident CTAs");
     if (TT::WC == 0) return TT::SMEM;
     const size_t per_sm = 228 * 1024;
@@ -650,15 +685,15 @@ size_t tm_smem() {
 }
 
 template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM = 0, int SY = 0,
-          int ST = kTmStages>
+          int ST = kTmStages, int TI = 0>
 void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
                const float* den, const Layout& L, const Weights<float>& W,
                const TiledContext& ctx, cudaStream_t st) {
-    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ, DM, SY, ST>;
+    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ, DM, SY, ST, TI>;
     static std::atomic<bool> configured[64];
     int dev = 0;
     cudaGetDevice(&dev);
-    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ, ST>();
+    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ, ST, TI>();
     if (!configured[dev & 63]) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[dev & 63] = true;
@@ -669,36 +704,42 @@ void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
     const int chunk = tm_chunk(ty, tx, nzi, R, MINB);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
+    const long long prev_slot = (up - ctx.u_base) / ctx.slot_stride;
     TmBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
              ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
     TmDamp F{ctx.damp_tz, ctx.damp_tx, ctx.damp_ty, ctx.damp, ctx.damp_faces_ok};
     PairWeights PW = pair_weights(W);
+    TmInterior maps_in;
+    std::memcpy(&maps_in.up, ctx.map_up_tm, sizeof(CUtensorMap));
+    std::memcpy(&maps_in.c, ctx.map_c_tm, sizeof(CUtensorMap));
+    std::memcpy(&maps_in.q, ctx.map_q_tm, sizeof(CUtensorMap));
     dim3 grid(ty, tx, zsplit);
     kernel<<<grid, 32 * XW, smem, st>>>(
         *reinterpret_cast<const CUtensorMap*>(ctx.map_u_tm),
-        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), un, uc, up, coefC, den,
-        ctx.coefGz, ctx.coefQ, F, L, PW, ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), maps_in, un, uc, up, coefC, den,
+        ctx.coefGz, ctx.coefQ, F, L, PW, ctx.inv_dt, (int)cur_slot, (int)prev_slot, chunk, zb,
+        ctx.err);
 }
 
 // Kernel configuration of the TMEM policies: u queue, density z term,
 // damping source, stage release and stage count
 // (SIMWAVE_TM_VARIANT="uq,rz,dm,sy,st" overrides it for measurements).
 struct TmVariant {
-    int uq = 1, rz = 0, dm = 0, sy = 0, st = 3;
+    int uq = 1, rz = 0, dm = 0, sy = 0, st = 3, ti = 0;
 };
 TmVariant tm_variant() {
     static TmVariant v = [] {
         TmVariant t;
         if (const char* e = std::getenv("SIMWAVE_TM_VARIANT")) {
-            int a = 1, b = 0, c = 0, d = 0, f = 3;
-            const int n = std::sscanf(e, "%d,%d,%d,%d,%d", &a, &b, &c, &d, &f);
-            if (n >= 2 && a >= 0 && a <= 1 && b >= 0 && b <= 3 && c >= 0 && c <= 2 &&
-                d >= 0 && d <= 1 && (f == 3 || f == 4 || f == 6)) {
+            int a = 1, b = 0, c = 0, d = 0, f = 3, g = 0;
+            const int n = std::sscanf(e, "%d,%d,%d,%d,%d,%d", &a, &b, &c, &d, &f, &g);
+            if (n >= 2) {
                 t.uq = a;
                 t.rz = b;
                 t.dm = c;
                 t.sy = d;
                 t.st = f;
+                t.ti = g;
             }
         }
         return t;
@@ -706,36 +747,40 @@ TmVariant tm_variant() {
     return v;
 }
 
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM>
-void launch_tm_sync(int sy, int stg, float* un, const float* uc, const float* up,
-                    const float* coefC, const float* den, const Layout& L,
-                    const Weights<float>& W, const TiledContext& ctx, cudaStream_t st) {
-    if (!sy) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);
-    if (stg == 6) return launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 6>(un, uc, up, coefC, den, L, W, ctx, st);
-    launch_tm<R, VD, XW, MINB, UQ, RZ, DM, 1, 4>(un, uc, up, coefC, den, L, W, ctx, st);
-}
-
+// The configurations measured on 12- and 16-row CTAs (u queue, density z
+// term, damping source, stage release, stages, TMA-staged operands); any
+// other request runs the default tensor-memory configuration.
 template <int R, bool VD, int XW, int MINB>
 void launch_tm_variant(float* un, const float* uc, const float* up, const float* coefC,
                        const float* den, const Layout& L, const Weights<float>& W,
                        const TiledContext& ctx, cudaStream_t st) {
     const TmVariant v = tm_variant();
-    int rz = v.rz;
-    if (rz == 2 && !ctx.coefGz) rz = 1;
-    if (R != 4 || !VD || XW != 12) {
-        launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
-        return;
+    auto is = [&](int uq, int rz, int dm, int sy, int stg, int ti) {
+        return v.uq == uq && v.rz == rz && v.dm == dm && v.sy == sy && v.st == stg &&
+               v.ti == ti && (rz != 2 || ctx.coefGz) && (!ti || ctx.tm_ti);
+    };
+    if constexpr (R == 4 && VD && MINB == 1) {
+        if constexpr (XW == 12) {
+            if (is(0, 2, 1, 1, 6, 0))
+                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 6, 0>(un, uc, up, coefC, den, L, W, ctx, st);
+            if (is(0, 3, 1, 1, 4, 0))
+                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 4, 0>(un, uc, up, coefC, den, L, W, ctx, st);
+            if (is(0, 2, 1, 1, 4, 1))
+                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+            if (is(0, 3, 1, 1, 4, 1))
+                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+            if (is(0, 2, 1, 1, 5, 1))
+                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 5, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+            if (is(0, 3, 1, 1, 5, 1))
+                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 5, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+        }
+        if constexpr (XW == 16) {
+            if (is(0, 2, 1, 1, 4, 1))
+                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+            if (is(0, 3, 1, 1, 4, 1))
+                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
+        }
     }
-#define SW_TMV(UQV, RZV)                                                                    \
-    if (v.uq == UQV && rz == RZV) {                                                         \
-        if (v.dm == 1) launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 1>(v.sy, v.st, un, uc, up,  \
-                                                                   coefC, den, L, W, ctx, st); \
-        else launch_tm_sync<R, VD, XW, MINB, UQV, RZV, 2>(v.sy, v.st, un, uc,                \
-                                                         up, coefC, den, L, W, ctx, st);     \
-        return;                                                                             \
-    }
-    SW_TMV(0, 3) SW_TMV(0, 2) SW_TMV(0, 1) SW_TMV(0, 0)
-#undef SW_TMV
     launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
 }
 
@@ -748,6 +793,8 @@ int tmem_rows(int policy) {
 }
 
 bool tmem_wants_density_z() { return tm_variant().rz == 2; }
+
+bool tmem_wants_interior() { return tm_variant().ti == 1; }
 
 void damp_face_tables(const float* damp, const Layout& L, const int* box, float* tz,
                       float* tx, float* ty, int* bad, cudaStream_t st) {

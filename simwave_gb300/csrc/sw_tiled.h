@@ -34,6 +34,11 @@ struct TiledContext {
     const float* damp_ty = nullptr;
     int damp_faces_ok = 0;         // tables match every one-axis-outside point
     float inv_dt = 0.f;
+    // boxes of the per-point operands (u_prev, C, Q) of the TMA-staged variant
+    alignas(64) unsigned char map_up_tm[128];
+    alignas(64) unsigned char map_c_tm[128];
+    alignas(64) unsigned char map_q_tm[128];
+    bool tm_ti = false;            // those descriptors encoded
 };
 
 // Encodes the descriptors; false when the layout or alignment does not suit
@@ -124,6 +129,10 @@ int resolve_policy(int policy, int r, bool vd);
 // nothing is launched).
 int tmem_rows(int policy);
 bool tmem_wants_density_z();
+bool tmem_wants_interior();
+// Encodes the u_prev / C / Q boxes of the TMA-staged variant once ctx.coefC
+// and ctx.coefQ exist; sets ctx.tm_ti.
+void tmem_encode_interior(TiledContext& ctx, const Layout& L, long long nslots);
 bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const float* uc,
                  const float* up, const float* coefC, const float* den, const Layout& L,
                  const Weights<float>& W, cudaStream_t st);
