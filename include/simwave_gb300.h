@@ -270,8 +270,14 @@ int simwave_forward_device(const simwave_problem *problem, void *stream);
                                            memory, damping from per-axis
                                            tables; 8 x rows per CTA, 2 CTAs
                                            per SM */
-#define SIMWAVE_POLICY_TMEM_WIDE 10     /* same, 16 x rows per CTA, 1 CTA per
-                                           SM */
+#define SIMWAVE_POLICY_STAGE_RELEASE 10 /* orders <= 8: packed arithmetic, u
+                                           queue in registers, density z term
+                                           from a per-run grid, 12 x rows per
+                                           CTA, 1 CTA per SM, six planes in
+                                           flight refilled by the last warp to
+                                           finish each (no CTA barrier per
+                                           plane); AUTO for order 8 with
+                                           variable density */
 int simwave_set_kernel_policy(int policy);
 
 /* How the host-pointer entries move grids (process-wide).

@@ -357,7 +357,6 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         }
         ctx.coefC = C;
         ctx.coefQ = Q;
-        if (tm) tmem_encode_interior(ctx, L, (long long)R.nslots);
         ctx.err = device_words() + 7;
         ctx.ok = true;
     }
@@ -1217,7 +1216,7 @@ extern "C" int simwave_device_status(void* stream) {
 }
 
 extern "C" int simwave_set_kernel_policy(int policy) {
-    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_TMEM_WIDE)
+    if (policy < SIMWAVE_POLICY_AUTO || policy > SIMWAVE_POLICY_STAGE_RELEASE)
         return SIMWAVE_E_ARGUMENT;
     sw::set_kernel_policy(policy);
     return SIMWAVE_OK;

@@ -284,7 +284,6 @@ static int run(const simwave_problem* P, cudaStream_t st) {
     ctx.err = words + 7;
     ctx.coefC = C;
     ctx.coefQ = Q;
-    if (ctx.tm) tmem_encode_interior(ctx, L, (long long)P->num_snapshots);
 
     // weights: unscaled half weights, per-axis 1/h^2 and 1/(4 h^2)
     const Weights<float> W = make_weights<float>(

@@ -1135,6 +1135,9 @@ void launch_vecp_any(float* un, const float* uc, const float* up, const float* c
 // 0.51; variable density only at order 10: 0.52 vs 0.63, its register
 // spills lose above), else the scalar kernel.
 int auto_policy(int r, bool vd) {
+    // order 8 with variable density (472^3 grid, ms per launch): the
+    // stage-release kernel 0.545, the packed kernel 0.555, the TMEM kernel 0.66
+    if (r == 4 && vd) return SIMWAVE_POLICY_STAGE_RELEASE;
     if (r <= 4) return (!vd && r == 1) ? SIMWAVE_POLICY_VEC_2CTA : SIMWAVE_POLICY_VEC_PACKED;
     if (r <= 8) {
         if (vd) return r == 5 ? SIMWAVE_POLICY_VEC_PACKED : SIMWAVE_POLICY_SCALAR_TILED;
@@ -1176,8 +1179,8 @@ void form_density_z(const float* den, float* gz, const Layout& L, const Weights<
 bool wants_density_z(const Layout& L, bool vd) {
     int p = kernel_policy();
     if (p == SIMWAVE_POLICY_AUTO) p = auto_policy(L.r, vd);
-    if ((p == SIMWAVE_POLICY_TMEM || p == SIMWAVE_POLICY_TMEM_WIDE) && L.r <= 4)
-        return vd && L.dim == 3 && tmem_wants_density_z();
+    if ((p == SIMWAVE_POLICY_TMEM || p == SIMWAVE_POLICY_STAGE_RELEASE) && L.r <= 4)
+        return vd && L.dim == 3 && p == SIMWAVE_POLICY_STAGE_RELEASE;
     return vd && L.dim == 3 && L.r <= 8 &&
            (p == SIMWAVE_POLICY_VEC_PACKED || p == SIMWAVE_POLICY_VEC_PACKED_1CTA);
 }
@@ -1239,7 +1242,7 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
     ctx.tm = false;
     const int pol = resolve_policy(kernel_policy(), r, vd);
     if (r <= 4 && (L.lead + r) % 4 == 0 &&
-        (pol == SIMWAVE_POLICY_TMEM || pol == SIMWAVE_POLICY_TMEM_WIDE)) {
+        (pol == SIMWAVE_POLICY_TMEM || pol == SIMWAVE_POLICY_STAGE_RELEASE)) {
         const int rows = tmem_rows(pol);
         const int vw = 128 + 2 * round4(r), vh = rows + 2 * r;
         CUtensorMap tu, trm;
@@ -1258,21 +1261,6 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
     return true;
 }
 
-void tmem_encode_interior(TiledContext& ctx, const Layout& L, long long nslots) {
-    ctx.tm_ti = false;
-    if (!ctx.tm || !ctx.coefC || !ctx.coefQ || !tmem_wants_interior()) return;
-    const int rows = ctx.tm_rows;
-    CUtensorMap mu, mc, mq;
-    if (encode_map(&mu, ctx.u_base, L, nslots, ctx.slot_stride, 128, rows) &&
-        encode_map(&mc, ctx.coefC, L, 1, L.nz * L.plane, 128, rows) &&
-        encode_map(&mq, ctx.coefQ, L, 1, L.nz * L.plane, 128, rows)) {
-        std::memcpy(ctx.map_up_tm, &mu, sizeof(mu));
-        std::memcpy(ctx.map_c_tm, &mc, sizeof(mc));
-        std::memcpy(ctx.map_q_tm, &mq, sizeof(mq));
-        ctx.tm_ti = true;
-    }
-}
-
 int resolve_policy(int policy, int r, bool vd) {
     return policy == SIMWAVE_POLICY_AUTO ? auto_policy(r, vd) : policy;
 }
@@ -1282,7 +1270,7 @@ int tiled_launch(const TiledContext& ctx, bool vd, float* un, const float* uc, c
                   const Weights<float>& W, float dt, float dt2, cudaStream_t st) {
     int policy = kernel_policy();
     const int resolved = resolve_policy(policy, L.r, vd);
-    if (resolved == SIMWAVE_POLICY_TMEM || resolved == SIMWAVE_POLICY_TMEM_WIDE) {
+    if (resolved == SIMWAVE_POLICY_TMEM || resolved == SIMWAVE_POLICY_STAGE_RELEASE) {
         if (tmem_launch(ctx, resolved, vd, un, uc, up, vel, den, L, W, st)) return resolved;
         policy = SIMWAVE_POLICY_VEC_PACKED;  // the context was prepared for another kernel
     }

@@ -1,38 +1,43 @@
-// sw_stencil_tmem.cu -- 3D float32 stencil, orders 2..8, whose z queues live
-// in tensor memory (sm_100 and later).
+// sw_stencil_tmem.cu -- 3D float32 stencils for orders 2..8 that stream
+// along z with their planes staged by TMA, in two configurations:
 //
-// Tiling as in the packed kernel of sw_stencil_tiled.cu: a CTA of XW warps
-// owns 128 (y) x XW (x) interior points and streams them along z over a chunk
-// of planes; lane l of warp w holds the y points y0 .. y0+3 (y0 = R + 128 bx +
-// 4 l) of the x row R + XW by + w. Per plane z:
-//   * the u tile and, with variable density, the density tile, each with an
-//     R-wide x/y halo, arrive in shared memory by TMA (cp.async.bulk.tensor,
-//     mbarrier completion), three planes deep: x and y derivatives;
-//   * the z derivatives come from per-thread rings of the 2R+1 planes
-//     z-R .. z+R held in tensor memory (TMEM): the thread's TMEM lane keeps
-//     one ring for u and one for the density, read with tcgen05.ld every
-//     plane; the ring head (plane z+R+1) is loaded from global memory a plane
-//     ahead and written with tcgen05.st into the slot plane z-R leaves. The
-//     rings cost no registers between planes, and the density's z term needs
-//     no per-point array of its own;
-//   * damping: where the mask is nonzero, its value comes from per-axis
-//     tables at points with exactly one axis outside the box where the mask
-//     is zero (tables taken from the mask's centre lines and checked on the
-//     device against every such point), and from the mask itself where two
-//     or three axes are outside (the layer's edges and corners); a mask that
-//     fails the check is read at every point outside the box. The update is
-//     written with t = damp C / dt:
-//       u_next = (2 - t) u - (1 - t) u_prev + C lap,
-//     the reference's 2/D u - N/D u_prev + value (dt^2/s)/D (D = 1 + q,
-//     N = 1 - q, q = damp dt / (2 s), C = (dt^2/s)/D, so 2/D = 2 - t and
-//     N/D = 1 - t); inside the box t = 0 and the arithmetic is the scalar
-//     update's;
-//   * arithmetic on 64-bit pairs (.f32x2): the derivative sums in the
-//     reference's order (c0 u first, then k = 1 .. R), the combine in the
-//     order y, x, z.
-// DRAM traffic per point update: u_cur, u_prev, C, density and u_next (20 B;
-// 16 B with constant density), plus the mask at the layer's edges and
-// corners.
+//   SIMWAVE_POLICY_TMEM: the z queues in tensor memory. The thread's TMEM
+//     lane keeps a ring of the 2R+1 planes z-R .. z+R of u and one of the
+//     density (tcgen05.ld every plane, the ring head written with
+//     tcgen05.st into the slot plane z-R leaves), so the rings cost no
+//     registers and the density's z term needs no per-point array; the
+//     damping mask comes from per-axis tables (below). 8 x rows per CTA, two
+//     CTAs per SM. Least DRAM traffic of the 3D kernels: 23.3 B per point
+//     update at order 8 with variable density (20 B algorithmic).
+//   SIMWAVE_POLICY_STAGE_RELEASE: u queue in registers, density z term from
+//     the per-point array gz formed once per run, damping from Q = damp dt /
+//     (2 s); 12 x rows per CTA (up to 168 registers a thread), one CTA per SM,
+//     six planes in flight, and no CTA barrier per plane: the last warp to
+//     finish reading a stage loads the plane six ahead into it (shared-memory
+//     acquire/release count, async-proxy fence), so warps drift by up to
+//     five planes. The default for order 8 with variable density.
+//
+// Common tiling (as the packed kernel of sw_stencil_tiled.cu): a CTA of XW
+// warps owns 128 (y) x XW (x) interior points and streams them along z over a
+// chunk of planes; lane l of warp w holds the y points y0 .. y0+3 (y0 = R +
+// 128 bx + 4 l) of the x row R + XW by + w. Per plane z the u tile and, with
+// variable density, the density tile, each with an R-wide x/y halo, arrive in
+// shared memory by TMA (cp.async.bulk.tensor, mbarrier completion): x and y
+// derivatives; arithmetic on 64-bit pairs (.f32x2), the derivative sums in
+// the reference's order (c0 u first, then k = 1 .. R), the combine in the
+// order y, x, z.
+//
+// Damping from tables (TMEM policy): where the mask is nonzero, its value
+// comes from per-axis tables at points with exactly one axis outside the box
+// where the mask is zero (tables taken from the mask's centre lines and
+// checked on the device against every such point), and from the mask itself
+// where two or three axes are outside (the layer's edges and corners); a mask
+// that fails the check is read at every point outside the box. The update is
+// written with t = damp C / dt:
+//   u_next = (2 - t) u - (1 - t) u_prev + C lap,
+// the reference's 2/D u - N/D u_prev + value (dt^2/s)/D (D = 1 + q, N = 1 - q,
+// q = damp dt / (2 s), C = (dt^2/s)/D, so 2/D = 2 - t and N/D = 1 - t); inside
+// the box t = 0 and the arithmetic is the scalar update's.
 //
 // Every mbarrier wait is bounded; on expiry the CTA records an error code,
 // drains its outstanding copies (also bounded), frees its TMEM and returns.
@@ -40,9 +45,6 @@
 
 #include <algorithm>
 #include <atomic>
-#include <cstdio>
-#include <cstdlib>
-#include <cstring>
 
 #include "simwave_gb300.h"
 #include "sw_pairs.cuh"
@@ -61,7 +63,7 @@ __host__ __device__ constexpr int pow2_at_least(int n) {
     return p;
 }
 
-template <int R, bool VD, int XW, int UQ = 1, int RZ = 0, int ST = kTmStages, int TI = 0>
+template <int R, bool VD, int XW, int UQ, int RZ, int ST>
 struct TmTile {
     static constexpr int HY = round4(R);
     static constexpr int TW = 128 + 2 * HY;  // floats per tile row
@@ -76,19 +78,8 @@ struct TmTile {
     static constexpr int WC = (UQ == 1 ? QC : 0) + ((VD && RZ == 0) ? QC : 0);
     static constexpr int NCOLS = pow2_at_least((XW / 4) * WC);  // per CTA
     static constexpr int NF = VD ? 2 : 1;
-    // TI: the per-point operands (u_prev, C, Q) of a plane arrive by TMA
-    // too, as 128 x XW boxes in the plane's stage
-    static constexpr int IN = 128 * XW;                       // floats of one box
-    static constexpr int SF = NF * STRIDE + (TI ? 3 * IN : 0);  // floats per stage
-    static constexpr size_t SMEM = (size_t)ST * SF * 4 +
-                                   ((VD && RZ == 1) ? (size_t)QN * 32 * XW * 16 : 0) + 256;
-};
-
-// Boxes of the per-point operands (kernel parameter of the TI kernels).
-struct TmInterior {
-    CUtensorMap up;  // the wavefield slots (4D: pitched row, x, z, slot)
-    CUtensorMap c;   // C
-    CUtensorMap q;   // Q
+    static constexpr int SF = NF * STRIDE;  // floats per stage
+    static constexpr size_t SMEM = (size_t)ST * SF * 4 + 256;
 };
 
 struct TmBox {  // interior box where the damping mask is zero
@@ -124,40 +115,36 @@ __device__ __forceinline__ V4 ring_at(const unsigned* r, int s) {
     return {pair_of(r[4 * s], r[4 * s + 1]), pair_of(r[4 * s + 2], r[4 * s + 3])};
 }
 
-// Where the z derivatives come from (template switches of the kernel):
+// Template switches of the kernel:
 //   UQ  u queue: 0 registers (slots static in the unrolled plane loop),
 //       1 a ring in tensor memory;
-//   RZ  density z term: 0 a ring in tensor memory, 1 a per-thread ring in
-//       shared memory, 2 the per-point array gz = s1_z sum_k c1_k (rho(z+k)
-//       - rho(z-k)) formed once per run (4 B more per point), 3 a queue in
-//       registers.
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM, int SY, int ST, int TI>
+//   RZ  density z term: 0 a ring in tensor memory, 2 the per-point array
+//       gz = s1_z sum_k c1_k (rho(z+k) - rho(z-k)) formed once per run;
+//   DM  damping: 0 the per-axis tables, 1 the per-point Q;
+//   SY  stage release: 0 a CTA barrier per plane, 1 the last warp to finish
+//       a stage refills it;
+//   ST  stages (planes in flight).
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM, int SY, int ST>
 __global__ void __launch_bounds__(32 * XW, MINB)
 stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
-               const __grid_constant__ CUtensorMap map_rho,
-               const __grid_constant__ TmInterior maps_in, float* un,
+               const __grid_constant__ CUtensorMap map_rho, float* un,
                const float* __restrict__ uc, const float* up,
                const float* __restrict__ coefC, const float* __restrict__ den,
                const float* __restrict__ gz, const float* __restrict__ coefQ, TmDamp F, Layout L,
-               PairWeights PW, float inv_dt,
-               int slot_cur, int slot_prev, int zchunk, TmBox zb, int* __restrict__ err) {
-    using TT = TmTile<R, VD, XW, UQ, RZ, ST, TI>;
-    static_assert(!TI || DM == 1, "TMA-staged operands carry Q, not the damping tables");
+               PairWeights PW, float inv_dt, int slot_cur, int zchunk, TmBox zb,
+               int* __restrict__ err) {
+    using TT = TmTile<R, VD, XW, UQ, RZ, ST>;
+    static_assert(RZ == 0 || RZ == 2, "density z term");
     constexpr int S = ST;  // stages (planes in flight per field)
     constexpr int HY = TT::HY, TW = TT::TW, NC = TT::NC, QN = TT::QN, QC = TT::QC;
     constexpr int NF = TT::NF;
-    constexpr int NT = 32 * XW;
     constexpr bool TM_U = UQ == 1;
     constexpr bool TM_R = VD && RZ == 0;
-    constexpr bool SM_R = VD && RZ == 1;
     constexpr bool GZ_R = VD && RZ == 2;
-    constexpr bool RG_R = VD && RZ == 3;
     constexpr bool USE_TMEM = TM_U || TM_R;
-    // stages: u tile, density tile, then (TI) the u_prev, C and Q boxes
+    // stages: the u tile, then the density tile
     float* tiles = reinterpret_cast<float*>(sw_dyn_smem);  // [stages][SF]
-    float4* sq_base = reinterpret_cast<float4*>(tiles + S * TT::SF);
-    unsigned long long* bars =
-        reinterpret_cast<unsigned long long*>(sq_base + (SM_R ? QN * NT : 0));
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(tiles + S * TT::SF);
     int* words = reinterpret_cast<int*>(bars + S);
     int& s_abort = words[0];
     unsigned& s_tmem = *reinterpret_cast<unsigned*>(words + 1);
@@ -215,25 +202,12 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         tbase + ((unsigned)(32 * (warp & 3)) << 16) + (unsigned)((warp >> 2) * TT::WC);
     const unsigned tr = tu + (TM_U ? QC : 0);
 
-    // TI: the CTA's whole tile lies in the zero box on plane p (no Q box)
-    const bool tile_xy_in = (R + blockIdx.y * XW >= zb.x0) && (R + (blockIdx.y + 1) * XW <= zb.x1) &&
-                            (yb >= zb.y0) && (yb + 128 <= zb.y1);
-    auto tile_in_box = [&](int p) { return tile_xy_in && p >= zb.z0 && p < zb.z1; };
     auto issue = [&](int plane, int stage) {
         last_it[stage] = plane - zbeg;
         float* sb = tiles + stage * TT::SF;
-        const bool q = TI && !tile_in_box(plane);
-        mbar_expect_tx(&bars[stage],
-                       NF * TT::BYTES + (TI ? (2 + (q ? 1 : 0)) * TT::IN * 4 : 0));
+        mbar_expect_tx(&bars[stage], NF * TT::BYTES);
         tma_load_4d(sb, &map_u, &bars[stage], col0, row0, plane, slot_cur);
         if (VD) tma_load_4d(sb + TT::STRIDE, &map_rho, &bars[stage], col0, row0, plane, 0);
-        if (TI) {
-            float* si = sb + NF * TT::STRIDE;
-            const int ci = (int)L.lead + yb, ri = R + blockIdx.y * XW;
-            tma_load_4d(si, &maps_in.up, &bars[stage], ci, ri, plane, slot_prev);
-            tma_load_4d(si + TT::IN, &maps_in.c, &bars[stage], ci, ri, plane, 0);
-            if (q) tma_load_4d(si + 2 * TT::IN, &maps_in.q, &bars[stage], ci, ri, plane, 0);
-        }
     };
     if (threadIdx.x == 0)
         for (int i = 0; i < S && zbeg + i < zend; i++) issue(zbeg + i, i);
@@ -251,8 +225,6 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
 
     // queues and rings: plane p sits in slot (p - zbeg + R) mod QN
     V4 qu[TM_U ? 1 : QN];
-    V4 qr[RG_R ? QN : 1];
-    float4* sq = sq_base + threadIdx.x;
     {
         const float* pu = uc + (long long)(zbeg - R) * L.plane + offl;
         const float* pr = den + (long long)(zbeg - R) * L.plane + offl;
@@ -262,8 +234,6 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             if (TM_U) tmem_st_v4(tu + 4 * j, a);
             else qu[j] = a;
             if (TM_R) tmem_st_v4(tr + 4 * j, ldg_v4(pr, true));
-            if (SM_R) sts_v4(sq + j * NT, ldg_v4(pr, true));
-            if (RG_R) qr[j] = ldg_v4(pr, true);
             pu += L.plane;
             pr += L.plane;
         }
@@ -288,36 +258,17 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
     }
     const bool colin = xin && yinm == 15u;
     const unsigned flags = yinm | (gzi << 4) | (gzo << 8) | ((unsigned)xin << 12);
-    // DM 2: the thread's face values with z inside the box, held in registers
-    float dzi[4] = {0.f, 0.f, 0.f, 0.f};
-    if (DM == 2 && F.ok) {
-        const float txv = __ldg(F.tx + xl);
-#pragma unroll
-        for (int v = 0; v < 4; v++) {
-            const bool yo = !((yinm >> v) & 1u);
-            if (yo != !xin) dzi[v] = !xin ? txv : __ldg(F.ty + min(y0 + v, (int)L.ny - 1));
-        }
-    }
 
     // per-point operands of the next plane, fetched a plane ahead (p: the
     // plane's element offset of this thread's first point)
-    V4 nprev, ncoef, ngz = vzero(), nq = vzero(), ng = vzero();
-    float ntz = 0.f;
+    V4 nprev, ncoef, ngz = vzero(), nq = vzero();
     bool nbox = true;
     auto fetch = [&](int zz, long long p) {
-        if (!TI) {
-            nprev = ld_v4(up + p, true);
-            ncoef = ldg_v4(coefC + p, true);
-        }
+        nprev = ld_v4(up + p, true);
+        ncoef = ldg_v4(coefC + p, true);
         if (GZ_R) ngz = ldg_v4(gz + p, true);
         nbox = colin && zz >= zb.z0 && zz < zb.z1;
-        if (DM == 1 && !TI) nq = ldg_v4(coefQ + p, !nbox);
-        if (DM == 2 && !nbox) {  // the z table and the mask of the next plane
-            const bool zin = zz >= zb.z0 && zz < zb.z1;
-            const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
-            ntz = (!zin && F.ok) ? __ldg(F.tz + zz) : 0.f;
-            ng = ldg_v4(F.damp + p, need != 0);
-        }
+        if (DM == 1) nq = ldg_v4(coefQ + p, !nbox);
     };
     long long zoff = (long long)zbeg * L.plane + offl;  // this plane's offset
     fetch(zbeg, zoff);
@@ -334,9 +285,7 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             aborted_at = it;
             return false;
         }
-        V4 vprev = nprev, vcoef = ncoef, vq = nq;
-        const V4 vgz = ngz, vg = ng;
-        const float vtz = ntz;
+        const V4 vprev = nprev, vcoef = ncoef, vq = nq, vgz = ngz;
         const bool inbox = nbox;
 
         unsigned ur[TM_U ? QC : 1];
@@ -348,7 +297,7 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
         if (more) {  // queue heads (plane z+R+1) and the next plane's operands
             const long long ph = pz + (long long)(R + 1) * L.plane;
             hu = ldg_v4(uc + ph, true);
-            if (TM_R || SM_R || RG_R) hr = ldg_v4(den + ph, true);
+            if (TM_R) hr = ldg_v4(den + ph, true);
             fetch(z + 1, zoff);
         }
 
@@ -371,12 +320,6 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             const float* sb = tiles + stage * TT::SF;
             const float* tus = sb + (warp + R) * TW + 4 * lane;
             const float* trs = sb + TT::STRIDE + (warp + R) * TW + 4 * lane;
-            if (TI) {  // this plane's operands from its stage
-                const float* si = sb + NF * TT::STRIDE + warp * 128 + 4 * lane;
-                vprev = lds_v4(si);
-                vcoef = lds_v4(si + TT::IN);
-                if (!inbox) vq = lds_v4(si + 2 * TT::IN);
-            }
             // y axis of u on pairs: even offsets straight from the 16-byte
             // loads, odd offsets repacked once
             V4 sdy, fuy;
@@ -445,11 +388,7 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                     cross = {fma2(fuz.lo, vgz.lo, cross.lo), fma2(fuz.hi, vgz.hi, cross.hi)};
                 } else {
                     if (TM_R) tmem_wait_ld<QC>(rr);
-                    auto rq = [&](int d) -> V4 {
-                        if constexpr (TM_R) return ring_at(rr, slot(d));
-                        else if constexpr (RG_R) return qr[slot(d)];
-                        else return lds_v4(sq + slot(d) * NT);
-                    };
+                    auto rq = [&](int d) -> V4 { return ring_at(rr, slot(d)); };
                     V4 frz = vzero();
 #pragma unroll
                     for (int k = 1; k <= R; k++) frz = vw(k == 1, k, vsub(rq(k), rq(-k)), frz);
@@ -475,21 +414,6 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
                                                       rcp_approx(1.f + qq.z), rcp_approx(1.f + qq.w)));
                     a = {mul2(a.lo, rq.lo), mul2(a.hi, rq.hi)};
                 }
-            } else if (DM == 2 && !inbox) {
-                const bool zin = z >= zb.z0 && z < zb.z1;
-                const unsigned need = (flags >> (zin ? 4 : 8)) & 15u;
-                const float4 g4 = to_f4(vg);
-                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
-                float d[4];
-#pragma unroll
-                for (int v = 0; v < 4; v++)
-                    d[v] = ((need >> v) & 1u) ? gg[v] : (zin ? dzi[v] : vtz);
-                const V4 dv = from_f4(make_float4(d[0], d[1], d[2], d[3]));
-                const P2 idt = pk(inv_dt, inv_dt);
-                const V4 t = {mul2(mul2(dv.lo, vcoef.lo), idt), mul2(mul2(dv.hi, vcoef.hi), idt)};
-                const P2 one{PW.one}, two{PW.two};
-                a = {fma2(sub2(t.lo, one), vprev.lo, mul2(sub2(two, t.lo), u0.lo)),
-                     fma2(sub2(t.hi, one), vprev.hi, mul2(sub2(two, t.hi), u0.hi))};
             } else if (inbox) {
                 const P2 m1{PW.minus_one};
                 a = {fma2(m1, vprev.lo, add2(u0.lo, u0.lo)), fma2(m1, vprev.hi, add2(u0.hi, u0.hi))};
@@ -537,8 +461,6 @@ stencil3d_tmem(const __grid_constant__ CUtensorMap map_u,
             if (TM_U) tmem_st_v4(tu + 4 * slot(-R), hu);
             else qu[slot(-R)] = hu;
             if (TM_R) tmem_st_v4(tr + 4 * slot(-R), hr);
-            if (SM_R) sts_v4(sq + slot(-R) * NT, hr);
-            if (RG_R) qr[slot(-R)] = hr;
         }
         if (SY) {
             // the warp is done with the stage: the last warp to finish it
@@ -636,10 +558,6 @@ __global__ void damp_tables_verify(const float* __restrict__ damp, Layout L, con
     if (__syncthreads_or(mismatch) && threadIdx.x == 0) atomicOr(bad, 1);
 }
 
-struct TmDeviceInfo {
-    int sms = 0;
-};
-
 int tm_sms() {
     static std::atomic<int> sms[64];
     int dev = 0;
@@ -674,9 +592,9 @@ int tm_chunk(int ty, int tx, int nzi, int R, int per_sm) {
 // Shared memory of a CTA: the tiles, padded so that no more than MINB CTAs
 // fit on an SM when they hold TMEM (their allocations must fit the SM's 512
 // columns).
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int ST, int TI>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int ST>
 size_t tm_smem() {
-    using TT = TmTile<R, VD, XW, UQ, RZ, ST, TI>;
+    using TT = TmTile<R, VD, XW, UQ, RZ, ST>;
     static_assert(TT::WC == 0 || MINB * TT::NCOLS <= 512, "TMEM columns of the resident CTAs");
     if (TT::WC == 0) return TT::SMEM;
     const size_t per_sm = 228 * 1024;
@@ -684,16 +602,15 @@ size_t tm_smem() {
     return std::max(TT::SMEM, floor);
 }
 
-template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM = 0, int SY = 0,
-          int ST = kTmStages, int TI = 0>
+template <int R, bool VD, int XW, int MINB, int UQ, int RZ, int DM, int SY, int ST>
 void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
                const float* den, const Layout& L, const Weights<float>& W,
                const TiledContext& ctx, cudaStream_t st) {
-    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ, DM, SY, ST, TI>;
+    auto kernel = stencil3d_tmem<R, VD, XW, MINB, UQ, RZ, DM, SY, ST>;
     static std::atomic<bool> configured[64];
     int dev = 0;
     cudaGetDevice(&dev);
-    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ, ST, TI>();
+    const size_t smem = tm_smem<R, VD, XW, MINB, UQ, RZ, ST>();
     if (!configured[dev & 63]) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured[dev & 63] = true;
@@ -704,97 +621,20 @@ void launch_tm(float* un, const float* uc, const float* up, const float* coefC,
     const int chunk = tm_chunk(ty, tx, nzi, R, MINB);
     const int zsplit = (nzi + chunk - 1) / chunk;
     const long long cur_slot = (uc - ctx.u_base) / ctx.slot_stride;
-    const long long prev_slot = (up - ctx.u_base) / ctx.slot_stride;
     TmBox zb{ctx.zero_box[0], ctx.zero_box[1], ctx.zero_box[2],
              ctx.zero_box[3], ctx.zero_box[4], ctx.zero_box[5]};
     TmDamp F{ctx.damp_tz, ctx.damp_tx, ctx.damp_ty, ctx.damp, ctx.damp_faces_ok};
     PairWeights PW = pair_weights(W);
-    TmInterior maps_in;
-    std::memcpy(&maps_in.up, ctx.map_up_tm, sizeof(CUtensorMap));
-    std::memcpy(&maps_in.c, ctx.map_c_tm, sizeof(CUtensorMap));
-    std::memcpy(&maps_in.q, ctx.map_q_tm, sizeof(CUtensorMap));
     dim3 grid(ty, tx, zsplit);
     kernel<<<grid, 32 * XW, smem, st>>>(
         *reinterpret_cast<const CUtensorMap*>(ctx.map_u_tm),
-        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), maps_in, un, uc, up, coefC, den,
-        ctx.coefGz, ctx.coefQ, F, L, PW, ctx.inv_dt, (int)cur_slot, (int)prev_slot, chunk, zb,
-        ctx.err);
-}
-
-// Kernel configuration of the TMEM policies: u queue, density z term,
-// damping source, stage release and stage count
-// (SIMWAVE_TM_VARIANT="uq,rz,dm,sy,st" overrides it for measurements).
-struct TmVariant {
-    int uq = 1, rz = 0, dm = 0, sy = 0, st = 3, ti = 0;
-};
-TmVariant tm_variant() {
-    static TmVariant v = [] {
-        TmVariant t;
-        if (const char* e = std::getenv("SIMWAVE_TM_VARIANT")) {
-            int a = 1, b = 0, c = 0, d = 0, f = 3, g = 0;
-            const int n = std::sscanf(e, "%d,%d,%d,%d,%d,%d", &a, &b, &c, &d, &f, &g);
-            if (n >= 2) {
-                t.uq = a;
-                t.rz = b;
-                t.dm = c;
-                t.sy = d;
-                t.st = f;
-                t.ti = g;
-            }
-        }
-        return t;
-    }();
-    return v;
-}
-
-// The configurations measured on 12- and 16-row CTAs (u queue, density z
-// term, damping source, stage release, stages, TMA-staged operands); any
-// other request runs the default tensor-memory configuration.
-template <int R, bool VD, int XW, int MINB>
-void launch_tm_variant(float* un, const float* uc, const float* up, const float* coefC,
-                       const float* den, const Layout& L, const Weights<float>& W,
-                       const TiledContext& ctx, cudaStream_t st) {
-    const TmVariant v = tm_variant();
-    auto is = [&](int uq, int rz, int dm, int sy, int stg, int ti) {
-        return v.uq == uq && v.rz == rz && v.dm == dm && v.sy == sy && v.st == stg &&
-               v.ti == ti && (rz != 2 || ctx.coefGz) && (!ti || ctx.tm_ti);
-    };
-    if constexpr (R == 4 && VD && MINB == 1) {
-        if constexpr (XW == 12) {
-            if (is(0, 2, 1, 1, 6, 0))
-                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 6, 0>(un, uc, up, coefC, den, L, W, ctx, st);
-            if (is(0, 3, 1, 1, 4, 0))
-                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 4, 0>(un, uc, up, coefC, den, L, W, ctx, st);
-            if (is(0, 2, 1, 1, 4, 1))
-                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-            if (is(0, 3, 1, 1, 4, 1))
-                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-            if (is(0, 2, 1, 1, 5, 1))
-                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 5, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-            if (is(0, 3, 1, 1, 5, 1))
-                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 5, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-        }
-        if constexpr (XW == 16) {
-            if (is(0, 2, 1, 1, 4, 1))
-                return launch_tm<R, VD, XW, MINB, 0, 2, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-            if (is(0, 3, 1, 1, 4, 1))
-                return launch_tm<R, VD, XW, MINB, 0, 3, 1, 1, 4, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-        }
-    }
-    launch_tm<R, VD, XW, MINB, 1, 0>(un, uc, up, coefC, den, L, W, ctx, st);
+        *reinterpret_cast<const CUtensorMap*>(ctx.map_rho_tm), un, uc, up, coefC, den,
+        ctx.coefGz, ctx.coefQ, F, L, PW, ctx.inv_dt, (int)cur_slot, chunk, zb, ctx.err);
 }
 
 }  // namespace
 
-int tmem_rows(int policy) {
-    if (policy != SIMWAVE_POLICY_TMEM_WIDE) return 8;
-    const char* e = std::getenv("SIMWAVE_TM_WIDE_ROWS");
-    return (e && std::atoi(e) == 12) ? 12 : 16;
-}
-
-bool tmem_wants_density_z() { return tm_variant().rz == 2; }
-
-bool tmem_wants_interior() { return tm_variant().ti == 1; }
+int tmem_rows(int policy) { return policy == SIMWAVE_POLICY_STAGE_RELEASE ? 12 : 8; }
 
 void damp_face_tables(const float* damp, const Layout& L, const int* box, float* tz,
                       float* tx, float* ty, int* bad, cudaStream_t st) {
@@ -807,25 +647,23 @@ void damp_face_tables(const float* damp, const Layout& L, const int* box, float*
 bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const float* uc,
                  const float* up, const float* coefC, const float* den, const Layout& L,
                  const Weights<float>& W, cudaStream_t st) {
-    if (!ctx.tm || L.r > 4 || !ctx.damp || !ctx.damp_tz) return false;
-    const bool wide = policy == SIMWAVE_POLICY_TMEM_WIDE;
-    if (wide != (ctx.tm_rows != 8)) return false;
-    if (ctx.tm_rows == 12) {
-        if (vd && L.r == 4) {
-            launch_tm_variant<4, true, 12, 1>(un, uc, up, coefC, den, L, W, ctx, st);
-            return true;
-        }
+    if (!ctx.tm || L.r > 4 || ctx.tm_rows != tmem_rows(policy)) return false;
+    if (policy == SIMWAVE_POLICY_STAGE_RELEASE) {
+        if (vd && !ctx.coefGz) return false;  // the run formed no gz
+#define SW_SR(RR)                                                                          \
+    case RR:                                                                               \
+        if (vd) launch_tm<RR, true, 12, 1, 0, 2, 1, 1, 6>(un, uc, up, coefC, den, L, W, ctx, st);  \
+        else launch_tm<RR, false, 12, 1, 0, 2, 1, 1, 6>(un, uc, up, coefC, den, L, W, ctx, st);    \
+        return true;
+        switch (L.r) { SW_SR(1) SW_SR(2) SW_SR(3) SW_SR(4) }
+#undef SW_SR
         return false;
     }
-#define SW_TM(RR)                                                                  \
-    case RR:                                                                       \
-        if (vd) {                                                                  \
-            if (wide) launch_tm_variant<RR, true, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st);  \
-            else launch_tm_variant<RR, true, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);        \
-        } else {                                                                   \
-            if (wide) launch_tm_variant<RR, false, 16, 1>(un, uc, up, coefC, den, L, W, ctx, st); \
-            else launch_tm_variant<RR, false, 8, 2>(un, uc, up, coefC, den, L, W, ctx, st);       \
-        }                                                                          \
+    if (!ctx.damp || !ctx.damp_tz) return false;
+#define SW_TM(RR)                                                                          \
+    case RR:                                                                               \
+        if (vd) launch_tm<RR, true, 8, 2, 1, 0, 0, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);   \
+        else launch_tm<RR, false, 8, 2, 1, 0, 0, 0, 3>(un, uc, up, coefC, den, L, W, ctx, st);     \
         return true;
     switch (L.r) { SW_TM(1) SW_TM(2) SW_TM(3) SW_TM(4) }
 #undef SW_TM

@@ -23,7 +23,7 @@ struct TiledContext {
     const float* coefQ = nullptr;
     const float* coefGz = nullptr; // density z term (variable density), or null
     void* scratch = nullptr;       // the run's coefficient/zero-box scratch
-    // kernel with its z queues in tensor memory (sw_stencil_tmem.cu)
+    // kernels of sw_stencil_tmem.cu (TMEM and stage-release policies)
     alignas(64) unsigned char map_u_tm[128];   // boxes of tm_rows x rows
     alignas(64) unsigned char map_rho_tm[128];
     bool tm = false;               // descriptors encoded
@@ -34,11 +34,6 @@ struct TiledContext {
     const float* damp_ty = nullptr;
     int damp_faces_ok = 0;         // tables match every one-axis-outside point
     float inv_dt = 0.f;
-    // boxes of the per-point operands (u_prev, C, Q) of the TMA-staged variant
-    alignas(64) unsigned char map_up_tm[128];
-    alignas(64) unsigned char map_c_tm[128];
-    alignas(64) unsigned char map_q_tm[128];
-    bool tm_ti = false;            // those descriptors encoded
 };
 
 // Encodes the descriptors; false when the layout or alignment does not suit
@@ -124,15 +119,10 @@ void set_kernel_policy(int policy);
 // The SIMWAVE_POLICY_* the tiled launch resolves `policy` to for radius r.
 int resolve_policy(int policy, int r, bool vd);
 
-// Tensor-memory kernel (sw_stencil_tmem.cu): x rows per CTA of a policy;
-// the launch, false when the context or the radius does not suit it (then
-// nothing is launched).
+// Kernels of sw_stencil_tmem.cu (SIMWAVE_POLICY_TMEM, _STAGE_RELEASE): x
+// rows per CTA of a policy; the launch, false when the context or the radius
+// does not suit it (then nothing is launched).
 int tmem_rows(int policy);
-bool tmem_wants_density_z();
-bool tmem_wants_interior();
-// Encodes the u_prev / C / Q boxes of the TMA-staged variant once ctx.coefC
-// and ctx.coefQ exist; sets ctx.tm_ti.
-void tmem_encode_interior(TiledContext& ctx, const Layout& L, long long nslots);
 bool tmem_launch(const TiledContext& ctx, int policy, bool vd, float* un, const float* uc,
                  const float* up, const float* coefC, const float* den, const Layout& L,
                  const Weights<float>& W, cudaStream_t st);

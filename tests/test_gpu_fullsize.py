@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 # SIMWAVE_POLICY_* of the kernel the default policy runs for order 8 with
 # variable density (the kernel the benchmark times)
-BENCH_KERNEL = 7  # SIMWAVE_POLICY_VEC_PACKED
+BENCH_KERNEL = 10  # SIMWAVE_POLICY_STAGE_RELEASE
 
 
 def _oracle(kw):

@@ -162,7 +162,7 @@ def test_repeated_calls_are_deterministic():
 
 POLICIES = {"auto": 0, "scalar_tiled": 1, "vec_2cta": 2, "vec_1cta": 3,
             "vec_smemq": 4, "vec_2cta_rot": 5, "vec_1cta_rot": 6, "vec_packed": 7,
-            "vec_packed_1cta": 8, "tmem": 9, "tmem_wide": 10}
+            "vec_packed_1cta": 8, "tmem": 9, "stage_release": 10}
 
 
 @pytest.mark.parametrize("policy", list(POLICIES))
@@ -249,14 +249,15 @@ def test_fused_step_sources_across_tiles(order, vd):
     assert_close(dp.shot_record_numpy(), rrec, np.float32, "fused-step shot record")
 
 
-@pytest.mark.parametrize("policy", ["tmem", "tmem_wide"])
+@pytest.mark.parametrize("policy", ["tmem", "stage_release"])
 @pytest.mark.parametrize("mask", ["perturbed_faces", "uniform", "none"])
 def test_tmem_kernel_damping_masks(policy, mask):
     """The tensor-memory kernel takes the damping mask from per-axis tables
     where one axis is outside the zero box, checked on the device against
     the mask: a mask whose faces differ from its centre lines (read at every
     point instead), a uniform mask (no zero box) and no damping layer (the
-    box is the whole grid) all match the oracle."""
+    box is the whole grid) all match the oracle; so does the stage-release
+    kernel (damping from Q) on the same masks."""
     from simwave_gb300.backend import _lib
     from simwave_gb300.device import DeviceProblem
     bc = ("null_dirichlet", "null_neumann", "none", "null_dirichlet",
