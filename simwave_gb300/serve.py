@@ -9,12 +9,15 @@ host when the shot completes.
   admitted 2D shots by ``epoch_steps`` time steps in one graph-captured
   sequence, and newly admitted shots join at the next epoch.
 * Other shots (3D, or float64) run through the device entry, each on a
-  low-priority stream of its own, shortest first (interior updates), up to
-  ``inflight`` at a time, while the 2D batch keeps stepping on its
-  high-priority stream: their blocks fill the SMs the batch's short launches
-  leave idle (between epochs the host waits for the batch), and the block
-  scheduler places the batch's blocks first as SMs free up. With
-  ``overlap=False`` they wait until no 2D shot is in the batch instead.
+  low-priority stream of its own, shortest first (interior updates): up to
+  ``inflight_beside_2d`` of them while the 2D batch keeps stepping on its
+  high-priority stream, up to ``inflight`` once no 2D shot is in the batch.
+  Beside the batch they fill the SMs its short launches leave idle (between
+  epochs the host waits for the batch); the block scheduler places the
+  batch's blocks first as SMs free up, but a 3D kernel's blocks hold their
+  SM's registers until they finish, so each 3D shot running beside the
+  batch slows its steps (hence the separate, smaller cap). With
+  ``overlap=False`` they wait until no 2D shot is in the batch.
 
 Latency of a request = completion time - arrival time (queueing, upload,
 compute and shot-record download included).
@@ -75,7 +78,8 @@ class ShotServer:
     """Serve requests with continuous batching on one GPU."""
 
     def __init__(self, hbm_budget=None, epoch_steps=64, inflight=3, device="cuda",
-                 tile_rows=None, reserve_bytes=0, stage_workers=2, tuning=None, overlap=True):
+                 tile_rows=None, reserve_bytes=0, stage_workers=2, tuning=None, overlap=True,
+                 inflight_beside_2d=1):
         self.device = torch.device(device)
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
@@ -91,6 +95,7 @@ class ShotServer:
         self.epoch_stream = torch.cuda.Stream(self.device, priority=hi)
         self.inflight = max(int(inflight), 1)
         self.overlap = bool(overlap)
+        self.inflight_2d = max(0, min(int(inflight_beside_2d), self.inflight))
         # one stream per stream-run shot in flight
         self.shot_streams = [torch.cuda.Stream(self.device, priority=lo)
                              for _ in range(self.inflight)]
@@ -179,10 +184,11 @@ class ShotServer:
 
     def _launch(self):
         """Queue the shortest admitted stream-run shots, each on a free shot
-        stream (with ``overlap=False``, none while the 2D batch has shots or
-        is about to get some)."""
+        stream, up to the cap for the batch's state (with ``overlap=False``,
+        none while the 2D batch has shots or is about to get some)."""
         busy2d = bool(self.active2d) or any(r.batchable for r in self.staging)
-        while self.ready and len(self.active) < self.inflight and (self.overlap or not busy2d):
+        cap = (self.inflight_2d if self.overlap else 0) if busy2d else self.inflight
+        while self.ready and len(self.active) < cap:
             req = min(self.ready, key=lambda r: r.updates)
             self.ready.remove(req)
             used = {id(s) for _, _, s in self.active}

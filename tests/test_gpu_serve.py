@@ -104,7 +104,7 @@ def test_3d_shots_overlap_2d_epochs_and_each_other():
         kw = random_problem(sw, 3, 8, i == 1, "none", 0, shape=(40, 44, 44),
                             tf=0.08, seed=300 + i, nrec=5)
         reqs.append(Request(kw, 0.0, tag="3d%d" % i))
-    server = ShotServer(epoch_steps=16, inflight=3)
+    server = ShotServer(epoch_steps=16, inflight=3, inflight_beside_2d=3)
     server.prepare(reqs)
     server.serve(reqs, timeout=300)
     server.close()
