@@ -315,7 +315,7 @@ static TiledContext prepare_tiled(const Run<T>& R, cudaStream_t st) {
         const size_t n = (size_t)(L.dim == 3 ? L.nz * L.plane : L.nz * L.pitch);
         const bool gz = L.dim == 3 && wants_density_z(L, R.vd);
         // tensor-memory kernel: per-axis tables of the damping mask
-        const bool tm = L.dim == 3 && ctx.tm;
+        const bool tm = L.dim == 3 && ctx.tm && ctx.tm_tables;
         const size_t ntab = tm ? (size_t)(L.nz + L.nx + L.ny + 32) : 0;
         void* scratch = nullptr;
         SW_CUDA(cudaMallocAsync(&scratch,

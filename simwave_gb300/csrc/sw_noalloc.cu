@@ -264,7 +264,7 @@ static int run(const simwave_problem* P, cudaStream_t st) {
     NA_CUDA(cudaGetLastError());
     find_zero_box(Q, L, words, st);
     NA_CUDA(cudaGetLastError());
-    if (ctx.tm) {
+    if (ctx.tm && ctx.tm_tables) {
         damp_face_tables(damp, L, words, tabs, tabs + L.nz, tabs + L.nz + L.nx, words + 8, st);
         NA_CUDA(cudaGetLastError());
     }
@@ -273,7 +273,7 @@ static int run(const simwave_problem* P, cudaStream_t st) {
     NA_CUDA(cudaStreamSynchronize(st));
     const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2] && box[5] > box[4];
     for (int i = 0; i < 6; i++) ctx.zero_box[i] = good ? box[i] : 0;
-    if (ctx.tm) {
+    if (ctx.tm && ctx.tm_tables) {
         ctx.damp = damp;
         ctx.damp_tz = tabs;
         ctx.damp_tx = tabs + L.nz;

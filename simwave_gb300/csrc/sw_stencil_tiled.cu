@@ -998,11 +998,14 @@ void launch_r(float* un, const float* uc, const float* up, const float* vel, con
         dt, dt2, (int)cur_slot, chunk, zb, ctx.err);
 }
 
-// Walk each axis line through the grid centre outwards while the mask is
-// zero; one thread per axis (in 2D the y range is [0, 1)).
+// Along each axis line through the grid centre, the run of zeros of the mask
+// around the centre: block a scans axis a (strided over its threads) for the
+// nearest nonzero on either side (shared-memory max / min); in 2D the y range
+// is [0, 1).
 __global__ void zero_box_lines(const float* __restrict__ damp, Layout L, int* box) {
-    const int a = threadIdx.x;
+    const int a = blockIdx.x;
     if (a >= 3) return;
+    __shared__ int below, above;  // nearest nonzero index below / above the centre
     const long long c[3] = {L.nz / 2, L.nx / 2, L.ny / 2};
     const long long n = L.extent(a);
     auto at = [&](long long i) {
@@ -1010,16 +1013,25 @@ __global__ void zero_box_lines(const float* __restrict__ damp, Layout L, int* bo
         idx[a] = i;
         return damp[L.dim == 3 ? L.at3(idx[0], idx[1], idx[2]) : L.at2(idx[0], idx[1])];
     };
-    long long lo = c[a], hi = c[a];
-    if (at(c[a]) != 0.f) {
-        box[2 * a] = 0;
-        box[2 * a + 1] = 0;
-        return;
+    if (threadIdx.x == 0) {
+        below = -1;
+        above = (int)n;
     }
-    while (lo - 1 >= 0 && at(lo - 1) == 0.f) lo--;
-    while (hi + 1 < n && at(hi + 1) == 0.f) hi++;
-    box[2 * a] = (int)lo;
-    box[2 * a + 1] = (int)hi + 1;
+    __syncthreads();
+    int lo = -1, hi = (int)n;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        if (i == c[a] || at(i) == 0.f) continue;
+        if (i < c[a]) lo = max(lo, (int)i);
+        else hi = min(hi, (int)i);
+    }
+    atomicMax(&below, lo);
+    atomicMin(&above, hi);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool centre_zero = at(c[a]) == 0.f;
+        box[2 * a] = centre_zero ? below + 1 : 0;
+        box[2 * a + 1] = centre_zero ? above : 0;
+    }
 }
 
 // Verify the candidate box: box[6] becomes nonzero if any point inside has a
@@ -1196,7 +1208,7 @@ void set_kernel_policy(int p) { g_policy = p; }
 
 void find_zero_box(const float* damp, const Layout& L, int* box, cudaStream_t st) {
     cudaMemsetAsync(box, 0, 7 * sizeof(int), st);
-    zero_box_lines<<<1, 32, 0, st>>>(damp, L, box);
+    zero_box_lines<<<3, 256, 0, st>>>(damp, L, box);
     zero_box_verify<<<device_info().sms * 4, 256, 0, st>>>(damp, L, box);
 }
 
@@ -1253,6 +1265,7 @@ bool tiled_prepare(TiledContext& ctx, const Layout& L, bool vd, float* u_base,
             std::memcpy(ctx.map_rho_tm, &trm, sizeof(trm));
             ctx.tm = true;
             ctx.tm_rows = rows;
+            ctx.tm_tables = pol == SIMWAVE_POLICY_TMEM;
         }
     }
     ctx.u_base = u_base;

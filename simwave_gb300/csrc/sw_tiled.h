@@ -27,7 +27,8 @@ struct TiledContext {
     alignas(64) unsigned char map_u_tm[128];   // boxes of tm_rows x rows
     alignas(64) unsigned char map_rho_tm[128];
     bool tm = false;               // descriptors encoded
-    int tm_rows = 8;               // x rows per CTA (8 or 16)
+    int tm_rows = 8;               // x rows per CTA (8 or 12)
+    bool tm_tables = false;        // the kernel reads the per-axis damping tables
     const float* damp = nullptr;   // the damping mask (pitched like u)
     const float* damp_tz = nullptr;  // mask along the zero box's centre lines
     const float* damp_tx = nullptr;

@@ -16,8 +16,11 @@ host when the shot completes.
   epochs the host waits for the batch); the block scheduler places the
   batch's blocks first as SMs free up, but a 3D kernel's blocks hold their
   SM's registers until they finish, so each 3D shot running beside the
-  batch slows its steps (hence the separate, smaller cap). With
-  ``overlap=False`` they wait until no 2D shot is in the batch.
+  batch slows its steps (measured on the served workload: one 3D shot
+  beside the batch took the 2D shots' p50 latency from about 0.5 s to
+  2.5 s), so by default none runs beside the batch and the 3D shots overlap
+  one another once it is empty. ``overlap=False`` keeps every stream-run
+  shot out while 2D shots are batched, whatever the caps.
 
 Latency of a request = completion time - arrival time (queueing, upload,
 compute and shot-record download included).
@@ -79,7 +82,7 @@ class ShotServer:
 
     def __init__(self, hbm_budget=None, epoch_steps=64, inflight=3, device="cuda",
                  tile_rows=None, reserve_bytes=0, stage_workers=2, tuning=None, overlap=True,
-                 inflight_beside_2d=1):
+                 inflight_beside_2d=0):
         self.device = torch.device(device)
         free, _ = torch.cuda.mem_get_info(self.device)
         self.budget = int(hbm_budget if hbm_budget is not None else 0.85 * free)
