@@ -817,6 +817,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=384,
                     help="model points per axis (default 384)")
+    ap.add_argument("--policy", type=int, default=0,
+                    help="SIMWAVE_POLICY_* of the 3D stencil (default 0: AUTO)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 96-shot batched leg")
     ap.add_argument("--served", action="store_true",
@@ -858,6 +860,10 @@ def main():
     from simwave_gb300.device import DeviceProblem
 
     torch.cuda.set_device(local)
+    if args.policy:
+        import ctypes
+        if _lib.load().simwave_set_kernel_policy(ctypes.c_int(args.policy)) != 0:
+            raise SystemExit("unknown kernel policy %d" % args.policy)
     kw = vd3d_arguments(timesteps=args.timesteps, n=args.n)
     pts, updates = interior_updates(kw)
     dp = DeviceProblem(kw, device="cuda:%d" % local)
@@ -906,12 +912,16 @@ def main():
         with open(peaks_path) as f:
             peak = float(json.load(f)["hbm_gbs"])
         peak_src = "measured"
+    # DRAM bytes per launch of the kernel that ran, from its ncu capture
+    # (profiles/stencil_traffic.json, keyed by SIMWAVE_POLICY_*)
+    kernel_policy = int(st.get("stencil_kernel", 0))
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "stencil_traffic.json")
-    if os.path.exists(tpath):
+    if os.path.exists(tpath) and args.n == 384:
         with open(tpath) as f:
-            t = json.load(f)
-        traffic = t.get("bytes_per_launch_full_size")
+            t = json.load(f).get("by_policy", {}).get(str(kernel_policy))
+        if t:
+            traffic = t.get("bytes_per_launch_full_size")
     del dp
     torch.cuda.empty_cache()
 
@@ -990,6 +1000,7 @@ def main():
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": peak_src,
                          "kernel_ms": round(stencil_ms, 4),
+                         "kernel_policy": kernel_policy,
                          "bytes_per_launch": bytes_per_launch},
             "e2e": e2e,
             "gpu_launches": int(launches),

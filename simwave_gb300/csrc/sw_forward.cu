@@ -791,6 +791,13 @@ static double host_forward(const HostArgs<T>& A) {
         SW_CUDA(cudaMemcpyAsync(dst, sout[b], dense_bytes, cudaMemcpyDeviceToHost, cout));
         SW_CUDA(cudaEventRecord(ar.event(EV_OUT + b), cout));
     };
+    // with the trace: device time from the call's first upload to the first
+    // step and across the time loop
+    cudaEvent_t tr_ev[3] = {nullptr, nullptr, nullptr};
+    if (trace) {
+        for (auto& e : tr_ev) SW_CUDA(cudaEventCreate(&e));
+        SW_CUDA(cudaEventRecord(tr_ev[0], cin));
+    }
     // models and KWS tables first, then the slots in the order the steps
     // first touch them
     upload_grid(dvel, A.vel);
@@ -872,7 +879,9 @@ static double host_forward(const HostArgs<T>& A) {
         for (int p : done_at[i]) emit(p);
     };
     stamp("uploads queued");
+    if (trace) SW_CUDA(cudaEventRecord(tr_ev[1], st));
     dispatch_steps<T>(R, S, st, stats, nullptr);
+    if (trace) SW_CUDA(cudaEventRecord(tr_ev[2], st));
     stamp("steps queued");
 
     // slots that changed identity without being written
@@ -892,6 +901,14 @@ static double host_forward(const HostArgs<T>& A) {
     SW_CUDA(cudaStreamSynchronize(cin));
     SW_CUDA(cudaStreamSynchronize(cout));
     stamp("all done");
+    if (trace) {
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, tr_ev[0], tr_ev[1]);
+        cudaEventElapsedTime(&b, tr_ev[1], tr_ev[2]);
+        std::fprintf(stderr, "simwave host entry: device: uploads start -> loop start %.3f ms, "
+                             "time loop %.3f ms\n", a, b);
+        for (auto& e : tr_ev) cudaEventDestroy(e);
+    }
     pins.release();
     stamp("unpinned");
     check_device_words(st);
