@@ -637,6 +637,55 @@ static void fault_in(void* p, size_t bytes) {
     for (auto& t : th) t.join();
 }
 
+// Whether the halo of one dense host grid (every point with an index within
+// r of an edge) is zero bit for bit; the planes are scanned from all host
+// cores (3D) or by one thread (2D).
+template <typename T>
+static bool halo_is_zero(const T* g, int dim, size_t nz, size_t nx, size_t ny, size_t r) {
+    using W = typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type;
+    const W* w = reinterpret_cast<const W*>(g);
+    auto zero = [](const W* p, size_t n) {
+        W acc = 0;
+        for (size_t i = 0; i < n; i++) acc |= p[i];
+        return acc == 0;
+    };
+    if (dim == 2) {  // rows of nx, z slowest
+        for (size_t i = 0; i < nz; i++) {
+            const W* row = w + i * nx;
+            if (i < r || i >= nz - r) {
+                if (!zero(row, nx)) return false;
+            } else if (!zero(row, r) || !zero(row + nx - r, r)) {
+                return false;
+            }
+        }
+        return true;
+    }
+    auto plane_ok = [&](size_t i) {
+        const W* pl = w + i * nx * ny;
+        if (i < r || i >= nz - r) return zero(pl, nx * ny);
+        for (size_t j = 0; j < nx; j++) {
+            const W* row = pl + j * ny;
+            if (j < r || j >= nx - r) {
+                if (!zero(row, ny)) return false;
+            } else if (!zero(row, r) || !zero(row + ny - r, r)) {
+                return false;
+            }
+        }
+        return true;
+    };
+    const unsigned n = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<char> ok(n, 1);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < n; t++)
+        th.emplace_back([&, t] {
+            for (size_t i = t; i < nz && ok[t]; i += n) ok[t] = plane_ok(i);
+        });
+    for (auto& t : th) t.join();
+    for (char c : ok)
+        if (!c) return false;
+    return true;
+}
+
 struct HostPins {
     std::vector<void*> mine;
     bool add(const void* p, size_t bytes) {
@@ -815,10 +864,14 @@ static double host_forward(const HostArgs<T>& A) {
     // physical slot p starts with host slot p; upload those the run reads or
     // returns, in first-use order
     std::vector<size_t> first_use(A.nslots, (size_t)-1), last_write(A.nslots, (size_t)-1);
+    std::vector<size_t> first_read(A.nslots, (size_t)-1), first_write(A.nslots, (size_t)-1);
     for (size_t i = 0; i < S.steps.size(); i++) {
         const int ps[3] = {S.steps[i].prev, S.steps[i].cur, S.steps[i].next};
         for (int q = 0; q < 3; q++)
             if (first_use[ps[q]] == (size_t)-1) first_use[ps[q]] = i;
+        for (int q = 0; q < 2; q++)
+            if (first_read[ps[q]] == (size_t)-1) first_read[ps[q]] = i;
+        if (first_write[ps[2]] == (size_t)-1) first_write[ps[2]] = i;
         last_write[S.steps[i].next] = i;
     }
     std::vector<int> inv(A.nslots);
@@ -831,8 +884,18 @@ static double host_forward(const HostArgs<T>& A) {
         if (needed[p]) order.push_back(p);
     std::stable_sort(order.begin(), order.end(),
                      [&](size_t a, size_t b) { return first_use[a] < first_use[b]; });
+    // a slot the steps write before they read it keeps only its halo from
+    // the host (every interior point is overwritten first); when that halo
+    // is zero bit for bit (Solver.forward's zero-filled u_full), the slot is
+    // cleared on the device instead of uploaded
     for (size_t p : order) {
-        upload_grid(du + p * L.slot, A.u + p * dense);
+        const bool written_first = first_write[p] != (size_t)-1 && first_write[p] < first_read[p];
+        if (written_first &&
+            halo_is_zero<T>(A.u + p * dense, A.dim, A.nz, A.nx, A.dim == 3 ? A.ny : 1, L.r)) {
+            SW_CUDA(cudaMemsetAsync(du + p * L.slot, 0, (size_t)L.slot * sizeof(T), cin));
+        } else {
+            upload_grid(du + p * L.slot, A.u + p * dense);
+        }
         SW_CUDA(cudaEventRecord(ar.event(EV_READY + p), cin));
         uploaded[p] = 1;
     }

@@ -131,3 +131,28 @@ def test_smallest_grids_and_halo_windows(dim, order, extent):
     ru, rrec = _port(kw)
     assert rel_l2(u, ru) <= 1e-4
     assert rel_l2(rec, rrec) <= 1e-4
+
+
+@pytest.mark.parametrize("dim, stride", [(2, 3), (3, 2), (3, 0)])
+def test_nonzero_initial_slots(dim, stride):
+    """Every wavefield slot starts with nonzero values, halo included: the
+    host entry uploads a slot the steps write before they read only when its
+    halo is not zero (else it clears the slot on the device), so both paths
+    must keep the reference's result, which carries the initial halo values
+    through the run."""
+    shape = (40, 56) if dim == 2 else (30, 34, 34)
+    kw = random_problem(sw, dim, 8, True, BCS[:2 * dim], stride, shape=shape, tf=0.05,
+                        seed=7, nrec=4)
+    rng = np.random.default_rng(11)
+    u0 = rng.standard_normal(kw["u_full"].shape).astype(kw["u_full"].dtype)
+    r = kw["space_order"] // 2
+    # the last slot keeps a zero halo (cleared on the device), the others not
+    last = u0[-1]
+    inner = tuple(slice(r, n - r) for n in last.shape)
+    keep = last[inner].copy()
+    last[...] = 0
+    last[inner] = keep
+    kw = dict(kw, u_full=u0)
+    u, rec = _host(kw)
+    ru, rrec = _port(kw)
+    assert rel_l2(u, ru) <= 1e-4 and rel_l2(rec, rrec) <= 1e-4
