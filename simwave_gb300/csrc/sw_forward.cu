@@ -638,8 +638,8 @@ static void fault_in(void* p, size_t bytes) {
 }
 
 // Whether the halo of one dense host grid (every point with an index within
-// r of an edge) is zero bit for bit; the planes are scanned from all host
-// cores (3D) or by one thread (2D).
+// r of an edge; with r = 0 the whole grid) is zero bit for bit; the planes
+// are scanned from all host cores (3D) or by one thread (2D).
 template <typename T>
 static bool halo_is_zero(const T* g, int dim, size_t nz, size_t nx, size_t ny, size_t r) {
     using W = typename std::conditional<sizeof(T) == 4, uint32_t, uint64_t>::type;
@@ -652,7 +652,7 @@ static bool halo_is_zero(const T* g, int dim, size_t nz, size_t nx, size_t ny, s
     if (dim == 2) {  // rows of nx, z slowest
         for (size_t i = 0; i < nz; i++) {
             const W* row = w + i * nx;
-            if (i < r || i >= nz - r) {
+            if (i < r || i >= nz - r || r == 0) {
                 if (!zero(row, nx)) return false;
             } else if (!zero(row, r) || !zero(row + nx - r, r)) {
                 return false;
@@ -662,7 +662,7 @@ static bool halo_is_zero(const T* g, int dim, size_t nz, size_t nx, size_t ny, s
     }
     auto plane_ok = [&](size_t i) {
         const W* pl = w + i * nx * ny;
-        if (i < r || i >= nz - r) return zero(pl, nx * ny);
+        if (i < r || i >= nz - r || r == 0) return zero(pl, nx * ny);
         for (size_t j = 0; j < nx; j++) {
             const W* row = pl + j * ny;
             if (j < r || j >= nx - r) {
@@ -888,10 +888,11 @@ static double host_forward(const HostArgs<T>& A) {
     // the host (every interior point is overwritten first); when that halo
     // is zero bit for bit (Solver.forward's zero-filled u_full), the slot is
     // cleared on the device instead of uploaded
+    // (a slot read first is cleared the same way when it is zero throughout)
     for (size_t p : order) {
         const bool written_first = first_write[p] != (size_t)-1 && first_write[p] < first_read[p];
-        if (written_first &&
-            halo_is_zero<T>(A.u + p * dense, A.dim, A.nz, A.nx, A.dim == 3 ? A.ny : 1, L.r)) {
+        if (halo_is_zero<T>(A.u + p * dense, A.dim, A.nz, A.nx, A.dim == 3 ? A.ny : 1,
+                            written_first ? (size_t)L.r : 0)) {
             SW_CUDA(cudaMemsetAsync(du + p * L.slot, 0, (size_t)L.slot * sizeof(T), cin));
         } else {
             upload_grid(du + p * L.slot, A.u + p * dense);
