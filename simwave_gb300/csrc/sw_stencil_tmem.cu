@@ -571,12 +571,22 @@ int tm_sms() {
 }
 
 // z chunk length: fill the machine in whole waves, counting the 2R-plane
-// warm-up of every chunk as the cost of splitting.
+// warm-up of every chunk as the cost of splitting, with chunks of at most
+// kMaxChunk planes. Long chunks lose more than their warm-up saves: columns
+// in the damping layer run slower than those inside, so over a long chunk
+// neighbouring columns drift apart in z and the halo rows each reads of the
+// other are no longer in L2. Measured on the 472^3 order-8 grid with
+// variable density (ms per launch, 2 .. 64 chunks of 464 planes): 0.724,
+// 0.606, 0.563, 0.545, 0.527 (12 chunks of 39 planes), 0.528, 0.530, 0.542,
+// 0.570, 0.591; a wave of whole columns streaming all 464 planes, 0.640.
+constexpr int kMaxChunk = 40;
+
 int tm_chunk(int ty, int tx, int nzi, int R, int per_sm) {
     const long long slots = (long long)std::max(per_sm, 1) * tm_sms();
-    int best = 1;
+    const int zs_min = std::min((nzi + kMaxChunk - 1) / kMaxChunk, 64);
+    int best = std::max(zs_min, 1);
     double best_cost = 1e300;
-    for (int zs = 1; zs <= 32 && zs <= nzi; zs++) {
+    for (int zs = std::max(zs_min, 1); zs <= std::max(32, zs_min) && zs <= nzi; zs++) {
         const long long ctas = (long long)ty * tx * zs;
         const long long waves = (ctas + slots - 1) / slots;
         const int chunk = (nzi + zs - 1) / zs;

@@ -199,6 +199,35 @@ def test_tiled_and_generic_kernels_agree(order, vd, policy):
     assert rel_l2(tiled_u, gen_u) < 2e-5
 
 
+@pytest.mark.parametrize("order", [4, 8])
+@pytest.mark.parametrize("vd", [False, True])
+def test_stage_release_many_columns(order, vd):
+    """The stage-release kernel (AUTO for order 8 with variable density) on
+    a grid with more columns of 128 x 12 interior points than there are SMs
+    (160 or 243 columns, so several waves of CTAs, each a chunk of planes),
+    against the oracle."""
+    from simwave_gb300.backend import _lib
+    from simwave_gb300.device import DeviceProblem
+    bc = ("null_neumann", "null_dirichlet", "none", "null_neumann",
+          "null_dirichlet", "none")
+    kw = random_problem(sw, 3, order, vd, bc, 3, shape=(14 - order, 958 - order, 254 - order),
+                        tf=0.03, seed=order, nrec=7, nsrc=2)
+    nz, nx, ny = kw["velocity_model"].shape
+    assert ((ny - order + 127) // 128) * ((nx - order + 11) // 12) >= 160
+    dp = DeviceProblem(kw)
+    lib = _lib.load()
+    assert lib.simwave_set_kernel_policy(POLICIES["stage_release"]) == 0
+    try:
+        st = dp.run()
+        dp.status()
+    finally:
+        lib.simwave_set_kernel_policy(0)
+    assert st["stencil_kernel"] == POLICIES["stage_release"]
+    ru, rrec = port_forward(kw)
+    assert_close(dp.u_full_numpy(), ru, np.float32, "stage-release wavefield")
+    assert_close(dp.shot_record_numpy(), rrec, np.float32, "stage-release shot record")
+
+
 @pytest.mark.parametrize("order", [2, 4, 8, 14, 20])
 @pytest.mark.parametrize("vd", [False, True])
 def test_tiled2d_and_generic_kernels_agree(order, vd):
