@@ -389,7 +389,7 @@ typedef struct simwave_stats {
 /* No reference counterpart (the reference returns only its wall time). */
 int simwave_last_stats(simwave_stats *out);
 
-/* ---- velocity gradient (2D, float32, constant density) ------------------
+/* ---- velocity gradient (2D, float32, constant or variable density) ------
  * No reference counterpart: the reference offers only the forward operator
  * (simwave/kernel/backend/compiler.py:128-130) and its middleware dispatches
  * only 'forward' (simwave/kernel/backend/middleware.py:103-105).
@@ -397,7 +397,9 @@ int simwave_last_stats(simwave_stats *out);
  * The gradient is that of J = sum(g * receivers) with respect to the
  * velocity grid, for a cotangent g of the shot record, through the exact
  * discrete forward loop (damping, KWS source and receiver windows, boundary
- * conditions), with dt, the damping mask and the windows held fixed. The
+ * conditions), with dt, the damping mask, the density and the windows held
+ * fixed. Variable density needs the tiled layout of simwave_layout()
+ * (SIMWAVE_E_ARGUMENT otherwise). The
  * forward starts from zero levels; `u`, `num_snapshots`, `saving_stride` and
  * `slot_stride` are not used. KWS windows must lie inside the interior
  * (SIMWAVE_E_ARGUMENT otherwise), and each interior extent must be at least
@@ -420,8 +422,8 @@ int simwave_gradient_forward(const simwave_problem *problem, size_t interval,
  * problem and interval) and `grad_receivers` (device, end_timestep rows of
  * num_receivers float32), writes dJ/dv into `grad_velocity` (device, one
  * grid in the problem's pitched layout; zero outside the interior). Needs
- * (interval + 8) grids of scratch, plus interval rows of the Dirichlet
- * lines when an edge is null_dirichlet. */
+ * (interval + 8) grids of scratch (+ 2 with variable density), plus
+ * interval rows of the Dirichlet lines when an edge is null_dirichlet. */
 int simwave_gradient_backward(const simwave_problem *problem, size_t interval,
                               const void *checkpoints, const void *grad_receivers,
                               void *grad_velocity, void *stream);

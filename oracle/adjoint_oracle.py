@@ -1,5 +1,5 @@
-"""Float64 adjoint-state velocity gradient of the 2D constant-density forward
-loop (TEST INFRASTRUCTURE ONLY).
+"""Float64 adjoint-state velocity gradient of the 2D forward loop, constant
+or variable density (TEST INFRASTRUCTURE ONLY).
 
 Only tests/ and bench.py's checks use this module; the product package never
 imports it. The reference has no adjoint (its compiler offers only the
@@ -16,6 +16,15 @@ step in numpy from the forward's sections
     u^(n+1) = B w    boundary conditions, x edges then z edges
                                                          (wave.c:274-393)
     rec[n-1] = R u^n  KWS gather of the current level     (wave.c:395-464)
+
+With variable density (simwave/kernel/backend/c_code/forward/
+variable_density/2d/wave.c:143-201) L becomes
+    A u = L u - sum_a G_a fd_a(u),  G_a = fd_a(rho) / (4 h_a^2 rho),
+    fd_a(f)(p) = sum_k c1_k (f(p + k e_a) - f(p - k e_a))
+at the interior points (rho read on the whole grid, G_a formed at the
+interior points only), and L^T in the recursion below becomes
+    A^T z = L^T z + sum_a fd_a(G_a z)   (z supported on the interior),
+the first differences being antisymmetric.
 
 The gradient of J(v) = sum(g * rec(v)) for a given g (the shot-record
 cotangent) follows the adjoint-state recursion, with mu^m the adjoint of the
@@ -41,19 +50,24 @@ _BC = {'none': 0, 'null_dirichlet': 1, 'null_neumann': 2}
 
 
 class Problem2D:
-    """The forward problem of middleware keyword arguments (2D, constant
-    density), in float64."""
+    """The forward problem of middleware keyword arguments (2D, constant or
+    variable density), in float64."""
 
     def __init__(self, kwargs):
         kw = _oracle._normalise(kwargs)
-        if kw['velocity_model'].ndim != 2 or 'density_model' in kw:
-            raise ValueError("2D constant-density problems only")
+        if kw['velocity_model'].ndim != 2:
+            raise ValueError("2D problems only")
         self.vel = np.asarray(kw['velocity_model'], dtype=np.float64)
+        den = kw.get('density_model')
+        self.den = None if den is None else np.asarray(den, dtype=np.float64)
         self.damp = np.asarray(kw['damping_mask'], dtype=np.float64)
         self.nz, self.nx = self.vel.shape
         self.order = int(kw['space_order'])
         self.r = self.order // 2
         self.c2 = np.asarray(kw['second_order_fd_coefficients'], dtype=np.float64)
+        self.c1 = None
+        if self.den is not None:
+            self.c1 = np.asarray(kw['first_order_fd_coefficients'], dtype=np.float64)
         self.dz, self.dx = float(kw['dz']), float(kw['dx'])
         self.dt = float(kw['dt'])
         self.bc = [int(b) for b in kw['boundary_condition']]
@@ -89,9 +103,58 @@ class Problem2D:
         p = object.__new__(Problem2D)
         p.__dict__.update(self.__dict__)
         p.vel = np.asarray(vel, dtype=np.float64)
+        p._G = None
         return p
 
     # -- operators -----------------------------------------------------------
+    def _fd(self, f, axis, interior):
+        """fd_axis(f): at the interior points (`interior`, zero elsewhere;
+        reads the halo) or, for f supported on the interior, at every point."""
+        r, nz, nx = self.r, self.nz, self.nx
+        if interior:
+            I, J = slice(r, nz - r), slice(r, nx - r)
+            s = np.zeros((nz - 2 * r, nx - 2 * r))
+            for k in range(1, r + 1):
+                if axis == 1:
+                    s = s + self.c1[k] * (f[I, r + k:nx - r + k] - f[I, r - k:nx - r - k])
+                else:
+                    s = s + self.c1[k] * (f[r + k:nz - r + k, J] - f[r - k:nz - r - k, J])
+            out = np.zeros((nz, nx))
+            out[I, J] = s
+            return out
+        fp = np.pad(f, r)
+        s = np.zeros((nz, nx))
+        for k in range(1, r + 1):
+            if axis == 1:
+                s = s + self.c1[k] * (fp[r:r + nz, r + k:r + k + nx] - fp[r:r + nz, r - k:r - k + nx])
+            else:
+                s = s + self.c1[k] * (fp[r + k:r + k + nz, r:r + nx] - fp[r - k:r - k + nz, r:r + nx])
+        return s
+
+    def density_terms(self):
+        """G_z, G_x at the interior points (zero elsewhere)."""
+        if getattr(self, '_G', None) is None:
+            h2 = (self.dz * self.dz, self.dx * self.dx)
+            self._G = tuple(self._fd(self.den, a, True) / (4.0 * h2[a] * self.den)
+                            for a in (0, 1))
+        return self._G
+
+    def op(self, u):
+        """A u: L u, less the density term with variable density."""
+        out = self.lap(u)
+        if self.den is not None:
+            for a, G in enumerate(self.density_terms()):
+                out = out - G * self._fd(u, a, True)
+        return out
+
+    def op_t(self, z):
+        """A^T z for z supported on the interior, at every grid point."""
+        out = self.lap_t(z)
+        if self.den is not None:
+            for a, G in enumerate(self.density_terms()):
+                out = out + self._fd(G * z, a, False)
+        return out
+
     def lap(self, u):
         """L u at the interior points (zero elsewhere); reads the halo."""
         r, nz, nx = self.r, self.nz, self.nx
@@ -206,7 +269,7 @@ class Problem2D:
         rec = np.zeros((self.end, self.nrec))
         for n in range(self.begin, self.end + 1):
             un, up = levels[-1], levels[-2]
-            w = (2.0 * un - N * up) / D + c * (self.lap(un) + self.source_field(n))
+            w = (2.0 * un - N * up) / D + c * (self.op(un) + self.source_field(n))
             nxt = np.zeros((nz, nx))
             nxt[I, J] = w[I, J]
             levels.append(self.boundary(nxt))
@@ -232,10 +295,10 @@ class Problem2D:
             for s, (zs, xs, k) in enumerate(self.rec):
                 lam[zs, xs] += k * g[m - 1, s]
             lam[I, J] += (2.0 / D[I, J]) * mu1[I, J] - (N[I, J] / D[I, J]) * mu2[I, J]
-            lam += self.lap_t(c * mu1)
+            lam += self.op_t(c * mu1)
             mu = self.boundary_t(lam)
             n = m - 1
-            term = self.dt * self.dt * (self.lap(at(n)) + self.source_field(n)) \
+            term = self.dt * self.dt * (self.op(at(n)) + self.source_field(n)) \
                 - self.damp * self.dt * (at(n) - at(n - 1))
             grad[I, J] += (mu * dvdD * term)[I, J]
             mu2, mu1 = mu1, mu

@@ -1,6 +1,7 @@
-// sw_gradient.cu -- velocity gradient of the 2D float32 constant-density
-// forward loop: a forward pass that keeps checkpoints and a reverse pass that
-// recomputes one segment of levels at a time and runs the discrete adjoint.
+// sw_gradient.cu -- velocity gradient of the 2D float32 forward loop,
+// constant or variable density: a forward pass that keeps checkpoints and a
+// reverse pass that recomputes one segment of levels at a time and runs the
+// discrete adjoint.
 //
 // The reference has no adjoint (its compiler offers only the forward
 // operator, simwave/kernel/backend/compiler.py:128-130). The forward step n
@@ -24,6 +25,15 @@
 //   dJ/dv = sum_m nu^m * 2 / (v^3 dt^2) * (w^m - 2 u^(m-1) + u^(m-2)),
 // where w^m equals u^m except on the Dirichlet lines, whose values before
 // the boundary conditions are saved during the recomputation.
+//
+// With variable density (variable_density/2d/wave.c:143-201) L is the
+// forward's A u = L u - sum_a G_a fd_a(u), G_a = fd_a(rho) / (4 h_a^2 rho)
+// at interior points (fd_a the first difference with the c1 weights), and
+// the adjoint update applies A^T nu = L nu + sum_a fd_a(G_a nu) (the first
+// differences are antisymmetric, nu has a zero halo); the Neumann fold adds
+// the halo point's first-difference term, +- sum_k c1_k (G_a nu)(mirror side)
+// (+ at the edge before the interior, - after it). The velocity derivative
+// is the same expression with A for L, so the gradient term is unchanged.
 //
 // Checkpoints: the pair (u^(n-1), u^n) before every `interval`-th step,
 // stored by the forward pass in a caller buffer; the reverse pass rebuilds
@@ -84,6 +94,24 @@ __global__ void gradient_factor(const float* __restrict__ vel, float* __restrict
     }
 }
 
+// G_a = s1_a fd_a(rho) / rho at interior points (zero elsewhere; the
+// arrays are cleared first): the density terms of the adjoint operator.
+__global__ void density_terms(const float* __restrict__ den, float* __restrict__ Gz,
+                              float* __restrict__ Gx, Layout L, Weights<float> W) {
+    const int r = L.r;
+    const long long j = r + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long i = r + blockIdx.y * (long long)blockDim.y + threadIdx.y;
+    if (j >= L.nx - r || i >= L.nz - r) return;
+    const long long p = L.at2(i, j);
+    float fz = 0.0f, fx = 0.0f;
+    for (int k = 1; k <= r; k++) {
+        fz += W.c1[k] * (den[p + k * L.pitch] - den[p - k * L.pitch]);
+        fx += W.c1[k] * (den[p + k] - den[p - k]);
+    }
+    Gz[p] = __fdiv_rn(W.s1[0] * fz, den[p]);
+    Gx[p] = __fdiv_rn(W.s1[1] * fx, den[p]);
+}
+
 // The ring of interior points next to the halo (the Dirichlet lines): the
 // rows z = r and z = nz-r-1 over the interior columns, then the columns
 // x = r and x = nx-r-1 over the rows strictly between those two.
@@ -117,11 +145,12 @@ __global__ void save_ring(const float* __restrict__ u, Layout L, float* __restri
 
 // Transposed boundary operation of one edge (after: edge 1, before: edge 0)
 // on the line at index `line` of the other axis. `nu1` is the previous
-// adjoint level (zero halo), read for L nu^(m+1) at the halo points.
+// adjoint level (zero halo), read for A^T nu^(m+1) at the halo points; `Ga`
+// the density term of `axis` (variable density) or null.
 __device__ __forceinline__ void fold_edge(float* __restrict__ nu, const float* __restrict__ nu1,
                                           const float* __restrict__ C, const Layout& L,
                                           const Weights<float>& W, int axis, long long line,
-                                          int edge, int type) {
+                                          int edge, int type, const float* __restrict__ Ga) {
     if (type == 0) return;
     const int r = L.r;
     const int other = axis == 0 ? 1 : 0;
@@ -141,7 +170,18 @@ __device__ __forceinline__ void fold_edge(float* __restrict__ nu, const float* _
         float lam = 0.0f;
         for (int k = q; k <= r; k++) lam += W.c2[k] * nu1[first + (k - q) * inward];
         const long long b = first + q * inward;
-        nu[b] += C[b] * (lam * ih2);
+        if (Ga) {
+            // the halo point's first difference reaches the interior on the
+            // inward side only: + before the interior, - after it
+            float d = 0.0f;
+            for (int k = q; k <= r; k++) {
+                const long long pk_ = first + (k - q) * inward;
+                d += W.c1[k] * (Ga[pk_] * nu1[pk_]);
+            }
+            nu[b] += C[b] * (lam * ih2 + (edge ? -d : d));
+        } else {
+            nu[b] += C[b] * (lam * ih2);
+        }
     }
 }
 
@@ -150,11 +190,11 @@ __device__ __forceinline__ void fold_edge(float* __restrict__ nu, const float* _
 // in the opposite order; they touch disjoint points).
 __global__ void fold_phase(float* __restrict__ nu, const float* __restrict__ nu1,
                            const float* __restrict__ C, Layout L, Weights<float> W, int axis,
-                           int before, int after) {
+                           int before, int after, const float* __restrict__ Ga) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= boundary_lines(L, axis)) return;
-    fold_edge(nu, nu1, C, L, W, axis, L.r + t, 1, after);
-    fold_edge(nu, nu1, C, L, W, axis, L.r + t, 0, before);
+    fold_edge(nu, nu1, C, L, W, axis, L.r + t, 1, after, Ga);
+    fold_edge(nu, nu1, C, L, W, axis, L.r + t, 0, before, Ga);
 }
 
 // Receiver transposes of table point t (receiver order within the point,
@@ -223,6 +263,7 @@ __global__ void accumulate_gradient(float* __restrict__ grad, const float* __res
 struct AdjointTiles {
     Layout L;
     const float *C, *Q, *K;
+    const float *Gz, *Gx;  // variable density: the density terms, else null
     Weights<float> W;
     int zb[4];
     int bc[4];
@@ -235,7 +276,7 @@ struct AdjointTiles {
 
 extern __shared__ __align__(16) float4 sw_grad_smem[];
 
-template <int R>
+template <int R, bool VD>
 __global__ void __launch_bounds__(batch::kThreads)
 adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* nu2,
                const float* g_row, const float* u_m, const float* u_m1, const float* u_m2,
@@ -243,8 +284,12 @@ adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* 
     const int t = blockIdx.x;
     const int tz = t / A.tiles_x, tx = t - (t / A.tiles_x) * A.tiles_x;
     const Layout& L = A.L;
-    batch::stencil2d_tile<R, false, 16>(reinterpret_cast<float*>(sw_grad_smem), L, num, nu1,
-                                        nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx);
+    if (VD)
+        batch::adjoint2d_density_tile<R, 16>(reinterpret_cast<float*>(sw_grad_smem), L, num,
+                                             nu1, nu2, A.C, A.Q, A.Gz, A.Gx, A.W, A.zb, tz, tx);
+    else
+        batch::stencil2d_tile<R, false, 16>(reinterpret_cast<float*>(sw_grad_smem), L, num, nu1,
+                                            nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx);
     __syncthreads();
     if (A.pts)
         for (int e = A.tile_ptr[t] + threadIdx.x; e < A.tile_ptr[t + 1]; e += blockDim.x)
@@ -256,15 +301,15 @@ adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* 
     // transposed order: z edges (the columns of this tile), then x edges
     if ((tz == A.tiles_z - 1 && A.bc[1]) || (tz == 0 && A.bc[0])) {
         for (int c = x0 + threadIdx.x; c < x1; c += blockDim.x) {
-            if (tz == A.tiles_z - 1) fold_edge(num, nu1, A.C, L, A.W, 0, c, 1, A.bc[1]);
-            if (tz == 0) fold_edge(num, nu1, A.C, L, A.W, 0, c, 0, A.bc[0]);
+            if (tz == A.tiles_z - 1) fold_edge(num, nu1, A.C, L, A.W, 0, c, 1, A.bc[1], A.Gz);
+            if (tz == 0) fold_edge(num, nu1, A.C, L, A.W, 0, c, 0, A.bc[0], A.Gz);
         }
     }
     __syncthreads();
     if ((tx == A.tiles_x - 1 && A.bc[3]) || (tx == 0 && A.bc[2])) {
         for (int i = z0 + threadIdx.x; i < z1; i += blockDim.x) {
-            if (tx == A.tiles_x - 1) fold_edge(num, nu1, A.C, L, A.W, 1, i, 1, A.bc[3]);
-            if (tx == 0) fold_edge(num, nu1, A.C, L, A.W, 1, i, 0, A.bc[2]);
+            if (tx == A.tiles_x - 1) fold_edge(num, nu1, A.C, L, A.W, 1, i, 1, A.bc[3], A.Gx);
+            if (tx == 0) fold_edge(num, nu1, A.C, L, A.W, 1, i, 0, A.bc[2], A.Gx);
         }
     }
     __syncthreads();
@@ -275,31 +320,56 @@ adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* 
     }
 }
 
-template <int R>
-static void adjoint_r(const AdjointTiles& A, float* num, const float* nu1, const float* nu2,
-                      const float* g_row, const float* u_m, const float* u_m1,
-                      const float* u_m2, const float* ring, cudaStream_t st) {
+// Tile stencil of the adjoint alone (the separate-kernel path): nu_next
+// from nu, nu_prev over 16 x 128 tiles.
+template <int R, bool VD>
+__global__ void __launch_bounds__(batch::kThreads)
+adjoint2d_tiles(const AdjointTiles A, float* num, const float* nu1, const float* nu2) {
+    const int t = blockIdx.x;
+    const int tz = t / A.tiles_x, tx = t - (t / A.tiles_x) * A.tiles_x;
+    if (VD)
+        batch::adjoint2d_density_tile<R, 16>(reinterpret_cast<float*>(sw_grad_smem), A.L, num,
+                                             nu1, nu2, A.C, A.Q, A.Gz, A.Gx, A.W, A.zb, tz, tx);
+    else
+        batch::stencil2d_tile<R, false, 16>(reinterpret_cast<float*>(sw_grad_smem), A.L, num,
+                                            nu1, nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx);
+}
+
+template <int R, bool VD>
+static void adjoint_r(const AdjointTiles& A, bool fused, float* num, const float* nu1,
+                      const float* nu2, const float* g_row, const float* u_m,
+                      const float* u_m1, const float* u_m2, const float* ring,
+                      cudaStream_t st) {
     constexpr int HX = (R + 3) & ~3;
-    const int bytes = (16 + 2 * R) * (128 + 2 * HX) * 4;
+    const int bytes = (VD ? 3 : 1) * (16 + 2 * R) * (128 + 2 * HX) * 4;
     static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
     int dev = 0;
     GR_CUDA(cudaGetDevice(&dev));
     if (!configured[dev & 63]) {
-        GR_CUDA(cudaFuncSetAttribute(adjoint2d_step<R>,
+        GR_CUDA(cudaFuncSetAttribute(adjoint2d_step<R, VD>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        GR_CUDA(cudaFuncSetAttribute(adjoint2d_tiles<R, VD>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         configured[dev & 63] = true;
     }
-    adjoint2d_step<R><<<A.tiles_x * A.tiles_z, batch::kThreads, bytes, st>>>(
-        A, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring);
+    if (fused)
+        adjoint2d_step<R, VD><<<A.tiles_x * A.tiles_z, batch::kThreads, bytes, st>>>(
+            A, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring);
+    else
+        adjoint2d_tiles<R, VD><<<A.tiles_x * A.tiles_z, batch::kThreads, bytes, st>>>(
+            A, num, nu1, nu2);
 }
 
-static void adjoint_launch(const AdjointTiles& A, float* num, const float* nu1,
+// The adjoint step in one launch (`fused`), or its tile stencil alone.
+static void adjoint_launch(const AdjointTiles& A, bool fused, float* num, const float* nu1,
                            const float* nu2, const float* g_row, const float* u_m,
                            const float* u_m1, const float* u_m2, const float* ring,
                            cudaStream_t st) {
-#define GR_A(RR)                                                                        \
-    case RR:                                                                            \
-        adjoint_r<RR>(A, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring, st);              \
+    const bool vd = A.Gz != nullptr;
+#define GR_A(RR)                                                                            \
+    case RR:                                                                                \
+        if (vd) adjoint_r<RR, true>(A, fused, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring, st); \
+        else adjoint_r<RR, false>(A, fused, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring, st);   \
         break;
     switch (A.L.r) {
         GR_A(1) GR_A(2) GR_A(3) GR_A(4) GR_A(5) GR_A(6) GR_A(7) GR_A(8) GR_A(9) GR_A(10)
@@ -332,6 +402,8 @@ struct Ctx {
     float dt;
     const float* vel;
     const float* damp;
+    const float* den = nullptr;  // variable density, else null
+    bool vd = false;
     const float* wavelet;
     size_t wavelet_count;
     Windows<float> src, rec;
@@ -393,9 +465,10 @@ static void check_interior_windows(const char* what, const HostWindows& H, size_
 
 static Ctx make_ctx(const simwave_problem* P, cudaStream_t st, HostWindows* rec_out) {
     if (!P) refuse(SIMWAVE_E_ARGUMENT, "null problem");
-    if (P->dim != 2 || P->variable_density || P->precision != 4)
-        refuse(SIMWAVE_E_ARGUMENT,
-               "the gradient supports 2D float32 constant-density problems");
+    if (P->dim != 2 || P->precision != 4)
+        refuse(SIMWAVE_E_ARGUMENT, "the gradient supports 2D float32 problems");
+    if (P->variable_density && (!P->density || !P->coeff_order1))
+        refuse(SIMWAVE_E_ARGUMENT, "variable density needs the density and the first-order weights");
     if (P->space_order < 2 || P->space_order > 2 * kMaxRadius || P->space_order % 2)
         refuse(SIMWAVE_E_ARGUMENT, "space_order must be even, 2..20");
     if (!P->velocity || !P->damp || !P->coeff_order2 || !P->boundary_conditions ||
@@ -443,7 +516,11 @@ static Ctx make_ctx(const simwave_problem* P, cudaStream_t st, HostWindows* rec_
                   R, st);
     check_interior_windows("receiver", R, P->num_receivers, X.L);
     if (rec_out) *rec_out = std::move(R);
-    X.W = make_weights<float>((const float*)P->coeff_order2, nullptr, r, P->dz, P->dx, 1.0);
+    X.vd = P->variable_density != 0;
+    X.den = X.vd ? (const float*)P->density : nullptr;
+    X.W = make_weights<float>((const float*)P->coeff_order2,
+                              X.vd ? (const float*)P->coeff_order1 : nullptr, r, P->dz, P->dx,
+                              1.0);
     X.dt = (float)P->dt;
     X.vel = (const float*)P->velocity;
     X.damp = (const float*)P->damp;
@@ -465,8 +542,14 @@ static void prepare_coefficients(Ctx& X, Scratch& mem, bool aligned) {
     X.Q = mem.get<float>((size_t)X.grid);
     form_coefficients(X.vel, X.damp, X.C, X.Q, X.grid, X.dt, mem.st);
     GR_LAUNCHED("form_coefficients");
-    X.tiled = aligned && tiled2d_supported(X.L);
-    if (!X.tiled) return;
+    X.tiled = aligned && tiled2d_supported(X.L) &&
+              (!X.vd || (reinterpret_cast<uintptr_t>(X.den) & 15) == 0);
+    if (!X.tiled) {
+        if (X.vd)
+            refuse(SIMWAVE_E_ARGUMENT,
+                   "the variable-density gradient needs the tiled layout (simwave_layout())");
+        return;
+    }
     int* words = mem.get<int>(16);
     find_zero_box(X.Q, X.L, words, mem.st);
     GR_LAUNCHED("find_zero_box");
@@ -475,7 +558,7 @@ static void prepare_coefficients(Ctx& X, Scratch& mem, bool aligned) {
     GR_CUDA(cudaStreamSynchronize(mem.st));
     const bool good = box[6] == 0 && box[1] > box[0] && box[3] > box[2];
     for (int i = 0; i < 6; i++) X.zero_box[i] = good ? box[i] : 0;
-    X.fused = shot2d_prepare(X.shot, X.L, X.C, X.Q, nullptr, X.vel, X.damp, X.W, X.zero_box,
+    X.fused = shot2d_prepare(X.shot, X.L, X.C, X.Q, X.den, X.vel, X.damp, X.W, X.zero_box,
                              X.src, X.wavelet, X.wavelet_count, X.dt, X.rec, X.receivers,
                              X.bc) &&
               X.shot.fused;
@@ -489,7 +572,7 @@ static void prepare_coefficients(Ctx& X, Scratch& mem, bool aligned) {
 static void stencil(const Ctx& X, float* un, const float* uc, const float* up,
                     cudaStream_t st) {
     if (X.tiled) {
-        tiled2d_launch(X.L, false, un, uc, up, X.C, X.Q, nullptr, X.W, X.zero_box, st);
+        tiled2d_launch(X.L, X.vd, un, uc, up, X.C, X.Q, X.den, X.W, X.zero_box, st);
         GR_LAUNCHED("stencil2d_single");
         return;
     }
@@ -508,7 +591,7 @@ static void forward_step(const Ctx& X, float* un, const float* uc, const float* 
                          size_t n, float* ring_row, float* rec_row, cudaStream_t st) {
     if (X.fused) {
         // the record goes to X.receivers + (n - 1) * count, where rec_row points
-        step2d_launch(rec_row ? X.shot : X.shot_quiet, false, un, uc, up, (long long)n, st,
+        step2d_launch(rec_row ? X.shot : X.shot_quiet, X.vd, un, uc, up, (long long)n, st,
                       ring_row);
         GR_LAUNCHED("stencil2d_step");
         return;
@@ -677,8 +760,22 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
     gradient_factor<<<1024, 256, 0, st>>>(X.vel, Kf, (long long)G, X.dt);
     GR_LAUNCHED("gradient_factor");
     const AdjointTable T = build_table(R, P->num_receivers, X.L, mem);
+    float *Gz = nullptr, *Gx = nullptr;
+    if (X.vd) {
+        Gz = mem.get<float>(2 * G);
+        Gx = Gz + G;
+        GR_CUDA(cudaMemsetAsync(Gz, 0, 2 * bytes, st));
+        const int rr = X.L.r;
+        const dim3 blk(32, 8, 1);
+        const dim3 grd((unsigned)((X.L.nx - 2 * rr + 31) / 32),
+                       (unsigned)((X.L.nz - 2 * rr + 7) / 8), 1);
+        density_terms<<<grd, blk, 0, st>>>(X.den, Gz, Gx, X.L, X.W);
+        GR_LAUNCHED("density_terms");
+    }
     AdjointTiles A{};
-    if (X.fused) {
+    if (X.tiled) {
+        A.Gz = Gz;
+        A.Gx = Gx;
         A.L = X.L;
         A.C = X.C;
         A.Q = X.Q;
@@ -721,13 +818,19 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
             const float* nu2 = nu + ((m + 2) % 3) * G;
             if (X.fused) {  // the whole adjoint step in one launch
                 const size_t k = m - n0;
-                adjoint_launch(A, num, nu1, nu2, g + (m - 1) * P->num_receivers,
+                adjoint_launch(A, true, num, nu1, nu2, g + (m - 1) * P->num_receivers,
                                seg + (k + 1) * G, seg + k * G, seg + (k - 1) * G,
                                ring ? ring + (m - 1 - n0) * (size_t)ring_len : nullptr, st);
                 GR_LAUNCHED("adjoint2d_step");
                 continue;
             }
-            stencil(X, num, nu1, nu2, st);
+            if (X.vd) {
+                adjoint_launch(A, false, num, nu1, nu2, nullptr, nullptr, nullptr, nullptr,
+                               nullptr, st);
+                GR_LAUNCHED("adjoint2d_tiles");
+            } else {
+                stencil(X, num, nu1, nu2, st);
+            }
             if (T.npts) {
                 adjoint_receivers<<<(unsigned)((T.npts + 255) / 256), 256, 0, st>>>(
                     num, X.C, T.pts, T.rowptr, T.rec, T.wt, g + (m - 1) * P->num_receivers,
@@ -740,7 +843,7 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
                 if (!b0 && !b1) continue;
                 const long long lines = boundary_lines(X.L, a);
                 fold_phase<<<(unsigned)((lines + 127) / 128), 128, 0, st>>>(
-                    num, nu1, X.C, X.L, X.W, a, b0, b1);
+                    num, nu1, X.C, X.L, X.W, a, b0, b1, a == 0 ? Gz : Gx);
                 GR_LAUNCHED("fold_phase");
             }
             const size_t k = m - n0;  // seg index of u^(m-1); u^m at k + 1

@@ -6,8 +6,9 @@ library) behind ``torch.autograd``.
 differentiable tensor; ``backward`` runs the discrete adjoint with
 checkpointed recomputation (a level pair every ``interval`` steps, ``interval``
 = ceil(sqrt(steps)) by default, so memory grows with sqrt(T) instead of T).
-2D float32 constant-density problems; the reference offers only the forward
-operator (simwave/kernel/backend/compiler.py:128-130).
+2D float32 problems, constant or variable density (the density is held
+fixed); the reference offers only the forward operator
+(simwave/kernel/backend/compiler.py:128-130).
 
 ``misfit_gradient(velocity, problems, observed)`` is the full-waveform
 inversion step: the L2 misfit 0.5 * sum((rec - obs)^2) over shots and its
@@ -77,8 +78,8 @@ def shot_record(velocity, problem, interval=None):
     float32, on the problem's device)."""
     if not isinstance(problem, DeviceProblem):
         raise TypeError("expected a DeviceProblem")
-    if problem.dim != 2 or problem.vd or problem.dtype.itemsize != 4:
-        raise ValueError("the gradient supports 2D float32 constant-density problems")
+    if problem.dim != 2 or problem.dtype.itemsize != 4:
+        raise ValueError("the gradient supports 2D float32 problems")
     steps = problem.timesteps
     return _ShotRecord.apply(velocity, problem, int(interval or default_interval(steps)))
 

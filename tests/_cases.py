@@ -112,17 +112,19 @@ def random_problem(sw, dim, order, vd, bc, stride, dtype=np.float32, n=32,
 
 
 def edge_problem(bc, order=4, shape=(22, 26), timesteps=160, seed=0,
-                 dtype=np.float64, damping=0.0, nsrc=1):
-    """Middleware kwargs of a small 2D constant-density problem whose waves
-    reach every edge many times: no damping layer (or a uniform ``damping``),
-    a source window near the centre and receiver windows on the first and
-    second interior lines of every edge (the lines the boundary conditions
-    act on). Window values are random; the wavelet is random per source."""
+                 dtype=np.float64, damping=0.0, nsrc=1, density=False):
+    """Middleware kwargs of a small 2D problem whose waves reach every edge
+    many times: no damping layer (or a uniform ``damping``), a source window
+    near the centre and receiver windows on the first and second interior
+    lines of every edge (the lines the boundary conditions act on). Window
+    values are random; the wavelet is random per source. ``density``: a
+    random density (1000-2500 kg/m^3) on the whole grid, halo included."""
     from simwave_gb300.frontend.fd import half_coefficients
     rng = np.random.default_rng(seed)
     nz, nx = shape
     r = order // 2
     vel = (1500.0 + 1000.0 * rng.random(shape)).astype(dtype)
+    den = (1000.0 + 1500.0 * rng.random(shape)).astype(dtype) if density else None
     h, dt = 10.0, 1.0e-3
 
     def windows(boxes):
@@ -148,7 +150,7 @@ def edge_problem(bc, order=4, shape=(22, 26), timesteps=160, seed=0,
     nslots = 3
     return dict(
         u_full=np.zeros((nslots,) + shape, dtype=dtype),
-        velocity_model=vel, density_model=None,
+        velocity_model=vel, density_model=den,
         damping_mask=np.full(shape, damping, dtype=dtype),
         wavelet=w.reshape(-1) if nsrc > 1 else w[:, 0].copy(),
         wavelet_size=timesteps, wavelet_count=nsrc,

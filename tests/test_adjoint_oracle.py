@@ -20,8 +20,9 @@ BC_MIXES = [
 
 @pytest.mark.parametrize("bc", BC_MIXES)
 @pytest.mark.parametrize("order", [2, 4, 8])
-def test_forward_matches_restatement(bc, order):
-    kw = edge_problem(bc, order, nsrc=2, damping=2e-5, timesteps=120)
+@pytest.mark.parametrize("density", [False, True])
+def test_forward_matches_restatement(bc, order, density):
+    kw = edge_problem(bc, order, nsrc=2, damping=2e-5, timesteps=120, density=density)
     p = adjoint_oracle.Problem2D(kw)
     levels, rec = p.forward()
     kk = dict(kw, u_full=kw["u_full"].copy(), shot_record=kw["shot_record"].copy())
@@ -37,8 +38,9 @@ def _functional(p, g, vel):
 
 @pytest.mark.parametrize("bc", BC_MIXES)
 @pytest.mark.parametrize("order", [4, 8])
-def test_gradient_matches_finite_differences(bc, order):
-    kw = edge_problem(bc, order, nsrc=2, damping=2e-5)
+@pytest.mark.parametrize("density", [False, True])
+def test_gradient_matches_finite_differences(bc, order, density):
+    kw = edge_problem(bc, order, nsrc=2, damping=2e-5, density=density)
     p = adjoint_oracle.Problem2D(kw)
     rng = np.random.default_rng(7)
     g = rng.standard_normal((kw["end_timestep"], kw["num_receivers"]))
@@ -50,12 +52,13 @@ def test_gradient_matches_finite_differences(bc, order):
 
 
 @pytest.mark.parametrize("bc", [BC_MIXES[3], BC_MIXES[4]])
-def test_gradient_pointwise_at_edges(bc):
+@pytest.mark.parametrize("density", [False, True])
+def test_gradient_pointwise_at_edges(bc, density):
     """Single points on and next to the lines the boundary conditions act
     on, where the transposed boundary operations matter."""
     order = 4
     r = order // 2
-    kw = edge_problem(bc, order, damping=2e-5, timesteps=120)
+    kw = edge_problem(bc, order, damping=2e-5, timesteps=120, density=density)
     p = adjoint_oracle.Problem2D(kw)
     rng = np.random.default_rng(3)
     g = rng.standard_normal((kw["end_timestep"], kw["num_receivers"]))
@@ -82,11 +85,12 @@ def test_gradient_zero_outside_interior():
     assert not grad[:, :r].any() and not grad[:, -r:].any()
 
 
-def test_front_end_problem_with_damping_layer():
+@pytest.mark.parametrize("density", [False, True])
+def test_front_end_problem_with_damping_layer(density):
     """A problem built by the front end (damping layer, Ricker wavelet, KWS
     windows of radius 4)."""
     import simwave_gb300 as sw
-    kw = random_problem(sw, 2, 8, False, "null_neumann", 0, dtype=np.float64,
+    kw = random_problem(sw, 2, 8, density, "null_neumann", 0, dtype=np.float64,
                         shape=(30, 34), tf=0.12, seed=5, nrec=6)
     p = adjoint_oracle.Problem2D(kw)
     rng = np.random.default_rng(2)

@@ -1,7 +1,8 @@
 """The GPU velocity gradient (hand-written adjoint behind torch.autograd)
 against the float64 adjoint-state gradient and against finite differences
-of the GPU forward; checkpoint intervals give the same gradient; the
-differentiable shot record is the plain forward's."""
+of the GPU forward, with constant and variable density; checkpoint
+intervals give the same gradient; the differentiable shot record is the
+plain forward's."""
 import numpy as np
 import pytest
 
@@ -52,9 +53,10 @@ def _as64(kw):
 
 @pytest.mark.parametrize("bc", BC_MIXES)
 @pytest.mark.parametrize("order", [4, 8, 16])
-def test_gradient_matches_float64_adjoint(bc, order):
+@pytest.mark.parametrize("density", [False, True])
+def test_gradient_matches_float64_adjoint(bc, order, density):
     kw = edge_problem(bc, order, shape=(40, 44), timesteps=200, dtype=np.float32,
-                      damping=2e-5)
+                      damping=2e-5, density=density)
     rng = np.random.default_rng(11)
     g = rng.standard_normal((kw["end_timestep"], kw["num_receivers"])).astype(np.float32)
     _, grad = _gpu_gradient(kw, g)
@@ -62,9 +64,10 @@ def test_gradient_matches_float64_adjoint(bc, order):
     assert rel_l2(grad, ref) <= GRAD_TOL
 
 
-def test_front_end_problem_gradient():
+@pytest.mark.parametrize("density", [False, True])
+def test_front_end_problem_gradient(density):
     """Damping layer, Ricker wavelet, radius-4 KWS windows, Neumann edges."""
-    kw = random_problem(sw, 2, 8, False, "null_neumann", 0, shape=(60, 70), tf=0.25,
+    kw = random_problem(sw, 2, 8, density, "null_neumann", 0, shape=(60, 70), tf=0.25,
                         seed=4, nrec=12)
     rng = np.random.default_rng(5)
     g = rng.standard_normal((kw["end_timestep"], kw["num_receivers"])).astype(np.float32)
@@ -86,9 +89,10 @@ def test_record_equals_plain_forward():
 
 
 @pytest.mark.parametrize("bc", [BC_MIXES[3], BC_MIXES[4]])
-def test_checkpoint_interval_does_not_change_gradient(bc):
+@pytest.mark.parametrize("density", [False, True])
+def test_checkpoint_interval_does_not_change_gradient(bc, density):
     kw = edge_problem(bc, 8, shape=(40, 44), timesteps=150, dtype=np.float32,
-                      damping=2e-5, nsrc=1)
+                      damping=2e-5, nsrc=1, density=density)
     rng = np.random.default_rng(1)
     g = rng.standard_normal((150, kw["num_receivers"])).astype(np.float32)
     grads = [_gpu_gradient(kw, g, interval)[1] for interval in (1, 7, 13, 150, 1000)]
@@ -96,13 +100,22 @@ def test_checkpoint_interval_does_not_change_gradient(bc):
         assert np.array_equal(grads[0], other)
 
 
-def test_gradient_matches_finite_differences():
+@pytest.mark.parametrize("density", [False, True])
+def test_gradient_matches_finite_differences(density):
     """Directional derivative of J = sum(g * rec) by central differences of
     the GPU forward (float32 records summed in float64)."""
     import torch
     from simwave_gb300.gradient import shot_record
     kw = edge_problem(BC_MIXES[3], 8, shape=(40, 44), timesteps=200, dtype=np.float32,
-                      damping=2e-5)
+                      damping=2e-5, density=density)
+    if density:
+        # a smooth density (a point-random one makes the float32 difference
+        # quotient too noisy for this bar; the float64 oracle, itself checked
+        # by central differences, covers rough densities)
+        z = np.linspace(0.0, 1.0, 40)[:, None]
+        x = np.linspace(0.0, 1.0, 44)[None, :]
+        kw["density_model"] = (1800.0 + 400.0 * np.sin(3.0 * z + 1.0) *
+                               np.cos(2.0 * x)).astype(np.float32)
     rng = np.random.default_rng(3)
     g = rng.standard_normal((200, kw["num_receivers"]))
     _, grad = _gpu_gradient(kw, g.astype(np.float32))
