@@ -160,10 +160,6 @@ stencil2d_batched(const Shot* __restrict__ shots, const TileRef* __restrict__ ti
                               S.Q, S.den, S.W, S.zb, t.tz, t.tx);
 }
 
-// ---- time-blocked 2D stencil (constant density) -----------------------------------
-constexpr int kTbThreads = 512;
-constexpr int kTbWarps = kTbThreads / 32;
-
 // 16-byte asynchronous copy global -> shared (zero-filled when !ok).
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -174,6 +170,201 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) 
 __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
+
+// ---- streamed 2D stencil (tall tiles) ----------------------------------------------
+// A CTA owns 128 interior columns (a strip) of CH consecutive interior rows
+// and streams down them: rows of u (and rho) with an HX column halo arrive
+// by cp.async in a shared-memory ring of NR = 2R + 2G rows (G = 8 RW rows a
+// group, RW rows per warp), one group ahead of the rows being computed, so
+// each row is staged once per strip (plus the 2R rows where chunks meet)
+// instead of once per overlapping 16-row tile. Per group: a CTA barrier (the
+// ring slots of the next group are free), the copies of the next group's
+// rows, a wait for the current group's, a barrier, then each warp computes
+// RW rows with the per-point arithmetic of stencil2d_tile, so the results
+// are bit-identical to the staged tiles'.
+template <int R, bool VD, int CH, int RW>
+__device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout& L, float* un,
+                                                      const float* uc, const float* up,
+                                                      const float* C, const float* Q,
+                                                      const float* den, const Weights<float>& W,
+                                                      const int* zb, int tz, int tx) {
+    constexpr int HX = (R + 3) & ~3;
+    constexpr int TW = 128 + 2 * HX;
+    constexpr int G = kWarps * RW;   // rows per group
+    constexpr int NR = 2 * R + 2 * G;  // ring rows
+    constexpr int NC = (4 + 2 * HX) / 4;
+    constexpr int CHK = TW / 4;  // 16-byte chunks per row
+    static_assert(CH % G == 0, "chunk height");
+    const int zbeg = R + tz * CH;
+    const int zend = min(zbeg + CH, (int)L.nz - R);
+    const int x0 = R + tx * 128;
+    const int col0 = (int)L.lead + x0 - HX;
+    const int pitch = (int)L.pitch;
+    const int nz = (int)L.nz;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = x0 + 4 * lane;
+    const int xlim = (int)L.nx - R;
+    const bool xbox = x >= zb[2] && x + 3 < zb[3];
+    const int zlast = zend - 1 + R;  // last row any group needs
+    float* rr = ring + (VD ? NR * TW : 0);  // density ring
+
+    // rows [a, b) (clipped to zlast) into their ring slots, one commit group
+    auto stage = [&](int a, int b) {
+        b = min(b, zlast + 1);
+        const int n = (b - a) * CHK;
+        for (int i = threadIdx.x; i < n; i += kThreads) {
+            const int row = a + i / CHK, ch = i - (i / CHK) * CHK;
+            const int col = col0 + 4 * ch;
+            const bool ok = row < nz && col + 3 < pitch;
+            const long long o = ok ? (long long)row * pitch + col : 0;
+            const int s = (row % NR) * TW + 4 * ch;
+            cp_async16(ring + s, uc + o, ok);
+            if (VD) cp_async16(rr + s, den + o, ok);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    P2 w2[R + 1], w1[R + 1];
+#pragma unroll
+    for (int k = 0; k <= R; k++) {
+        w2[k] = pk(W.c2[k], W.c2[k]);
+        w1[k] = pk(W.c1[k], W.c1[k]);
+    }
+    const P2 ihx = pk(W.ih2[1], W.ih2[1]), ihz = pk(W.ih2[0], W.ih2[0]);
+    const P2 one = pk(1.f, 1.f);
+
+    stage(zbeg - R, zbeg + G + R);
+    for (int zr = zbeg; zr < zend; zr += G) {
+        // per-point operands of this warp's rows
+        V4 cc[RW], pv[RW], qq[RW];
+        bool qzero[RW];
+#pragma unroll
+        for (int j = 0; j < RW; j++) {
+            const int z = zr + warp + j * kWarps;
+            const bool ok = z < zend && x < xlim;
+            const long long p = (long long)z * pitch + L.lead + x;
+            qzero[j] = xbox && z >= zb[0] && z < zb[1];
+            cc[j] = ldg_v4(C + p, ok);
+            pv[j] = ld_v4(up + p, ok);
+            qq[j] = ldg_v4(Q + p, ok && !qzero[j]);
+        }
+        __syncthreads();  // the previous group's rows are read: their slots are free
+        stage(zr + G + R, zr + 2 * G + R);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();  // every thread's copies of this group's rows have landed
+#pragma unroll
+        for (int j = 0; j < RW; j++) {
+            const int z = zr + warp + j * kWarps;
+            if (z >= zend || x >= xlim) continue;
+            auto row = [&](int zz) { return ring + (zz % NR) * TW + 4 * lane; };
+            auto rrow = [&](int zz) { return rr + (zz % NR) * TW + 4 * lane; };
+            const float* tu = row(z);
+            const float* tr = rrow(z);
+            const long long p = (long long)z * pitch + L.lead + x;
+            // z axis: rows z +- k of the ring, this lane's 4 columns
+            const V4 u0 = lds_v4(tu + HX);
+            V4 sz = vmul(w2[0], u0), gz, rz;
+#pragma unroll
+            for (int k = 1; k <= R; k++) {
+                const V4 a = lds_v4(row(z + k) + HX);
+                const V4 b = lds_v4(row(z - k) + HX);
+                sz = vfma(w2[k], vadd(a, b), sz);
+                if (VD) {
+                    gz = k == 1 ? vmul(w1[k], vsub(a, b)) : vfma(w1[k], vsub(a, b), gz);
+                    const V4 ra = lds_v4(rrow(z + k) + HX);
+                    const V4 rb = lds_v4(rrow(z - k) + HX);
+                    rz = k == 1 ? vmul(w1[k], vsub(ra, rb)) : vfma(w1[k], vsub(ra, rb), rz);
+                }
+            }
+            // x axis on pairs
+            V4 sx, gx, rx, rho;
+            {
+                P2 ev[2 * NC], od[2 * NC - 1];
+                YWindow<NC>::load(tu, ev, od);
+                P2 sh[2], gh[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    sh[h] = mul2(w2[0], h ? u0.hi : u0.lo);
+#pragma unroll
+                    for (int k = 1; k <= R; k++) {
+                        const P2 a = YWindow<NC>::at(ev, od, HX + 2 * h + k);
+                        const P2 b = YWindow<NC>::at(ev, od, HX + 2 * h - k);
+                        sh[h] = fma2(w2[k], add2(a, b), sh[h]);
+                        if (VD)
+                            gh[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), gh[h]);
+                    }
+                }
+                sx = {sh[0], sh[1]};
+                gx = {gh[0], gh[1]};
+                if (VD) {
+                    YWindow<NC>::load(tr, ev, od);
+                    rho = {ev[HX / 2], ev[HX / 2 + 1]};
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+#pragma unroll
+                        for (int k = 1; k <= R; k++) {
+                            const P2 a = YWindow<NC>::at(ev, od, HX + 2 * h + k);
+                            const P2 b = YWindow<NC>::at(ev, od, HX + 2 * h - k);
+                            gh[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), gh[h]);
+                        }
+                    }
+                    rx = {gh[0], gh[1]};
+                }
+            }
+            // reference order: x then z (constant_density/2d/wave.c:166)
+            V4 lap = vfma(ihz, sz, vmul(ihx, sx));
+            if (VD) {
+                const P2 s1x = pk(W.s1[1], W.s1[1]), s1z = pk(W.s1[0], W.s1[0]);
+                V4 cross = {mul2(s1x, mul2(gx.lo, rx.lo)), mul2(s1x, mul2(gx.hi, rx.hi))};
+                cross = {fma2(s1z, mul2(gz.lo, rz.lo), cross.lo),
+                         fma2(s1z, mul2(gz.hi, rz.hi), cross.hi)};
+                const float4 rr4 = to_f4(rho);
+                const V4 inv = from_f4(make_float4(rcp_approx(rr4.x), rcp_approx(rr4.y),
+                                                   rcp_approx(rr4.z), rcp_approx(rr4.w)));
+                lap = {fma2(sub2({0ull}, cross.lo), inv.lo, lap.lo),
+                       fma2(sub2({0ull}, cross.hi), inv.hi, lap.hi)};
+            }
+            // a = 2 u - (1 - q) u_prev;  b = a / (1 + q);  u_next = b + C lap
+            V4 av = {fma2(sub2(qq[j].lo, one), pv[j].lo, add2(u0.lo, u0.lo)),
+                     fma2(sub2(qq[j].hi, one), pv[j].hi, add2(u0.hi, u0.hi))};
+            if (!qzero[j]) {
+                const float4 q4 = to_f4(qq[j]);
+                const V4 rq = from_f4(make_float4(rcp_approx(1.f + q4.x), rcp_approx(1.f + q4.y),
+                                                  rcp_approx(1.f + q4.z), rcp_approx(1.f + q4.w)));
+                av = {mul2(av.lo, rq.lo), mul2(av.hi, rq.hi)};
+            }
+            const V4 out = {fma2(lap.lo, cc[j].lo, av.lo), fma2(lap.hi, cc[j].hi, av.hi)};
+            if (x + 3 < xlim) {
+                *reinterpret_cast<ulonglong2*>(un + p) = make_ulonglong2(out.lo.v, out.hi.v);
+            } else {
+                const float4 o = to_f4(out);
+                const float oa[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    if (x + v < xlim) un[p + v] = oa[v];
+            }
+        }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // nothing in flight at exit
+}
+
+template <int R, bool VD, int CH>
+__global__ void __launch_bounds__(kThreads)
+stencil2d_streamed(const Shot* __restrict__ shots, const TileRef* __restrict__ tiles) {
+    const TileRef t = tiles[blockIdx.x];
+    const Shot& S = shots[t.shot];
+    if (!active(S)) return;
+    float* un;
+    const float *uc, *up;
+    slot_ptrs(S, un, uc, up);
+    const Layout L = S.L;
+    stencil2d_stream_body<R, VD, CH, 2>(reinterpret_cast<float*>(sw_batch_smem), L, un, uc, up,
+                                        S.C, S.Q, S.den, S.W, S.zb, t.tz, t.tx);
+}
+
+// ---- time-blocked 2D stencil (constant density) -----------------------------------
+constexpr int kTbThreads = 512;
+constexpr int kTbWarps = kTbThreads / 32;
 
 // Copies the owned points [zlo, zhi) x [xlo, xhi) of a staged buffer (row
 // pitch tw, region origin zr0, xc0) to the same points of grid g.
@@ -723,11 +914,27 @@ static void launch_group_t(bool configure, const Shot* shots, const TileRef* til
     stencil2d_batched<R, VD, TZ><<<ntiles, kThreads, bytes, st>>>(shots, tiles);
 }
 
+// streamed tiles of CH rows (ring of 2R + 32 rows, 2 rows per warp a group)
+template <int R, bool VD, int CH>
+static void launch_stream_t(bool configure, const Shot* shots, const TileRef* tiles,
+                            int ntiles, cudaStream_t st) {
+    constexpr int HX = (R + 3) & ~3;
+    const int bytes = (VD ? 2 : 1) * (2 * R + 2 * kWarps * 2) * (128 + 2 * HX) * 4;
+    if (configure) {
+        cudaFuncSetAttribute(stencil2d_streamed<R, VD, CH>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        return;
+    }
+    stencil2d_streamed<R, VD, CH><<<ntiles, kThreads, bytes, st>>>(shots, tiles);
+}
+
 template <int R, bool VD>
 static void launch_group_r(bool configure, int tz, const Shot* shots, const TileRef* tiles,
                            int ntiles, cudaStream_t st) {
     if (tz == 8) launch_group_t<R, VD, 8>(configure, shots, tiles, ntiles, st);
     else if (tz == 32) launch_group_t<R, VD, 32>(configure, shots, tiles, ntiles, st);
+    else if (tz == 64) launch_stream_t<R, VD, 64>(configure, shots, tiles, ntiles, st);
+    else if (tz == 128) launch_stream_t<R, VD, 128>(configure, shots, tiles, ntiles, st);
     else launch_group_t<R, VD, 16>(configure, shots, tiles, ntiles, st);
 }
 
@@ -1799,8 +2006,9 @@ extern "C" int simwave_batch_release(simwave_batch* b, int shot_id) {
 extern "C" int simwave_batch_set_tile_rows(simwave_batch* b, int space_order, int rows) {
     return sw::batch::guarded([&] {
         if (!b || space_order < 2 || space_order > 20 || space_order % 2 ||
-            (rows != 8 && rows != 16 && rows != 32))
-            sw::batch::fail(SIMWAVE_E_ARGUMENT, "space_order even in 2..20, rows 8, 16 or 32");
+            (rows != 8 && rows != 16 && rows != 32 && rows != 64 && rows != 128))
+            sw::batch::fail(SIMWAVE_E_ARGUMENT,
+                            "space_order even in 2..20, rows 8, 16, 32, 64 or 128");
         std::lock_guard<std::mutex> lock(sw::batch::g_mutex);
         Engine* e = sw::batch::engine(b);
         e->tile_rows[space_order / 2] = rows;

@@ -40,7 +40,7 @@ def test_batch_matches_oracle():
         assert rel_l2(p.shot_record_numpy(), rrec) <= 1e-4
 
 
-@pytest.mark.parametrize("rows", [8, 16, 32])
+@pytest.mark.parametrize("rows", [8, 16, 32, 64, 128])
 def test_batch_tile_heights_agree(rows):
     from simwave_gb300.batch import BatchEngine, run_batch
     from simwave_gb300.device import DeviceProblem
@@ -59,6 +59,32 @@ def test_batch_tile_heights_agree(rows):
         assert rel_l2(p.u_full_numpy(), s.u_full_numpy()) <= 1e-5
         assert rel_l2(p.shot_record_numpy(), s.shot_record_numpy()) <= 1e-5
     eng.close()
+
+
+@pytest.mark.parametrize("rows", [64, 128])
+def test_streamed_tiles_bitwise_equal_staged_tiles(rows):
+    """Tall tiles streamed through a ring of rows give the 16-row staged
+    tiles' results bit for bit (the same per-point arithmetic), on shots of
+    every order with and without density, taller and wider than one tile."""
+    from simwave_gb300.batch import BatchEngine, run_batch
+    from simwave_gb300.device import DeviceProblem
+    rng = np.random.default_rng(21)
+    kws = []
+    for i, order in enumerate((2, 4, 8, 12, 16, 20)):
+        nz, nx = (int(v) for v in rng.integers(150, 330, size=2))
+        kws.append(random_problem(sw, 2, order, bool(i % 2), ("null_neumann", "none",
+                                  "null_dirichlet", "null_neumann"), 2, shape=(nz, nx),
+                                  tf=0.05, seed=30 + i, nsrc=2, nrec=9))
+    out = {}
+    for h in (16, rows):
+        eng = BatchEngine()
+        for order in (2, 4, 8, 12, 16, 20):
+            eng.set_tile_rows(order, h)
+        probs = run_batch([DeviceProblem(k) for k in kws], engine=eng)
+        out[h] = [(p.u_full_numpy(), p.shot_record_numpy()) for p in probs]
+        eng.close()
+    for (u1, r1), (u2, r2) in zip(out[16], out[rows]):
+        assert np.array_equal(u1, u2) and np.array_equal(r1, r2)
 
 
 def test_batch_admits_while_running():
@@ -271,7 +297,7 @@ def test_autotune_returns_a_valid_setting():
     tuning = autotune(probs, steps=16)
     assert set(tuning) == {int(k["space_order"]) for k in kws}
     for t in tuning.values():
-        assert t["rows"] in (8, 16, 32) and 1 <= t["depth"] <= 4
+        assert t["rows"] in (8, 16, 32, 64, 128) and 1 <= t["depth"] <= 4
     eng = BatchEngine()
     eng.apply(tuning)
     run_batch(probs, engine=eng)
