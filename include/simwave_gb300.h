@@ -352,8 +352,8 @@ int simwave_batch_remaining(simwave_batch *batch, int shot_id, int *steps);
  * an older level than the per-step kernels would have left in it. */
 int simwave_batch_release(simwave_batch *batch, int shot_id);
 /* Tuning: stencil tile height for one space order: 8, 16 or 32 rows staged
- * at once (with an R-row halo each), or 64 or 128 rows streamed through a
- * ring of 2R + 32 staged rows (each row staged once per tile). */
+ * at once (with an R-row halo each), or 64, 128 or 256 rows streamed
+ * through a ring of 64 staged rows (each row staged once per tile). */
 int simwave_batch_set_tile_rows(simwave_batch *batch, int space_order, int rows);
 /* Tuning: time-blocking depth for one space order -- 1 (default: a launch
  * per step), or 2..4 steps per launch where depth x space_order / 2 <= 36

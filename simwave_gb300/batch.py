@@ -17,7 +17,7 @@ import torch
 from .backend import _lib
 from .device import DeviceProblem
 
-TILE_ROWS = (8, 16, 32, 64, 128)
+TILE_ROWS = (8, 16, 32, 64, 128, 256)
 DEPTHS = (2, 3, 4)
 
 

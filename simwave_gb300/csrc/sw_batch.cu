@@ -160,6 +160,8 @@ stencil2d_batched(const Shot* __restrict__ shots, const TileRef* __restrict__ ti
                               S.Q, S.den, S.W, S.zb, t.tz, t.tx);
 }
 
+constexpr int kRing = 64;  // rows in the streamed stencil's ring
+
 // 16-byte asynchronous copy global -> shared (zero-filled when !ok).
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, bool ok) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -174,10 +176,11 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // ---- streamed 2D stencil (tall tiles) ----------------------------------------------
 // A CTA owns 128 interior columns (a strip) of CH consecutive interior rows
 // and streams down them: rows of u (and rho) with an HX column halo arrive
-// by cp.async in a shared-memory ring of NR = 2R + 2G rows (G = 8 RW rows a
-// group, RW rows per warp), one group ahead of the rows being computed, so
-// each row is staged once per strip (plus the 2R rows where chunks meet)
-// instead of once per overlapping 16-row tile. Per group: a CTA barrier (the
+// by cp.async in a shared-memory ring of kRing = 64 rows (a power of two at
+// least 2R + 2G, so a row's slot is one AND; G = 8 RW rows a group, RW rows
+// per warp), one group ahead of the rows being computed, so each row is
+// staged once per strip (plus the 2R rows where chunks meet) instead of
+// once per overlapping 16-row tile. Per group: a CTA barrier (the
 // ring slots of the next group are free), the copies of the next group's
 // rows, a wait for the current group's, a barrier, then each warp computes
 // RW rows with the per-point arithmetic of stencil2d_tile, so the results
@@ -191,7 +194,8 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
     constexpr int HX = (R + 3) & ~3;
     constexpr int TW = 128 + 2 * HX;
     constexpr int G = kWarps * RW;   // rows per group
-    constexpr int NR = 2 * R + 2 * G;  // ring rows
+    constexpr int NR = kRing;        // ring rows
+    static_assert(2 * R + 2 * G <= NR && (NR & (NR - 1)) == 0, "ring size");
     constexpr int NC = (4 + 2 * HX) / 4;
     constexpr int CHK = TW / 4;  // 16-byte chunks per row
     static_assert(CH % G == 0, "chunk height");
@@ -217,7 +221,7 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
             const int col = col0 + 4 * ch;
             const bool ok = row < nz && col + 3 < pitch;
             const long long o = ok ? (long long)row * pitch + col : 0;
-            const int s = (row % NR) * TW + 4 * ch;
+            const int s = (int)((unsigned)row & (NR - 1)) * TW + 4 * ch;
             cp_async16(ring + s, uc + o, ok);
             if (VD) cp_async16(rr + s, den + o, ok);
         }
@@ -233,21 +237,21 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
     const P2 ihx = pk(W.ih2[1], W.ih2[1]), ihz = pk(W.ih2[0], W.ih2[0]);
     const P2 one = pk(1.f, 1.f);
 
+    // per-point operands of row z, fetched one of this warp's rows ahead
+    V4 ncc, npv, nqq;
+    bool nqz = true;
+    auto fetch = [&](int z) {
+        const bool ok = z < zend && x < xlim;
+        const long long p = (long long)z * pitch + L.lead + x;
+        nqz = xbox && z >= zb[0] && z < zb[1];
+        ncc = ldg_v4(C + p, ok);
+        npv = ld_v4(up + p, ok);
+        nqq = ldg_v4(Q + p, ok && !nqz);
+    };
+
     stage(zbeg - R, zbeg + G + R);
+    fetch(zbeg + warp);
     for (int zr = zbeg; zr < zend; zr += G) {
-        // per-point operands of this warp's rows
-        V4 cc[RW], pv[RW], qq[RW];
-        bool qzero[RW];
-#pragma unroll
-        for (int j = 0; j < RW; j++) {
-            const int z = zr + warp + j * kWarps;
-            const bool ok = z < zend && x < xlim;
-            const long long p = (long long)z * pitch + L.lead + x;
-            qzero[j] = xbox && z >= zb[0] && z < zb[1];
-            cc[j] = ldg_v4(C + p, ok);
-            pv[j] = ld_v4(up + p, ok);
-            qq[j] = ldg_v4(Q + p, ok && !qzero[j]);
-        }
         __syncthreads();  // the previous group's rows are read: their slots are free
         stage(zr + G + R, zr + 2 * G + R);
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
@@ -255,9 +259,13 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
 #pragma unroll
         for (int j = 0; j < RW; j++) {
             const int z = zr + warp + j * kWarps;
+            V4 cc[1] = {ncc}, pv[1] = {npv}, qq[1] = {nqq};
+            const bool qzero[1] = {nqz};
+            // the next row of this warp (the next group's first, after the last)
+            fetch(z + kWarps);
             if (z >= zend || x >= xlim) continue;
-            auto row = [&](int zz) { return ring + (zz % NR) * TW + 4 * lane; };
-            auto rrow = [&](int zz) { return rr + (zz % NR) * TW + 4 * lane; };
+            auto row = [&](int zz) { return ring + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
+            auto rrow = [&](int zz) { return rr + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
             const float* tu = row(z);
             const float* tr = rrow(z);
             const long long p = (long long)z * pitch + L.lead + x;
@@ -325,15 +333,15 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
                        fma2(sub2({0ull}, cross.hi), inv.hi, lap.hi)};
             }
             // a = 2 u - (1 - q) u_prev;  b = a / (1 + q);  u_next = b + C lap
-            V4 av = {fma2(sub2(qq[j].lo, one), pv[j].lo, add2(u0.lo, u0.lo)),
-                     fma2(sub2(qq[j].hi, one), pv[j].hi, add2(u0.hi, u0.hi))};
-            if (!qzero[j]) {
-                const float4 q4 = to_f4(qq[j]);
+            V4 av = {fma2(sub2(qq[0].lo, one), pv[0].lo, add2(u0.lo, u0.lo)),
+                     fma2(sub2(qq[0].hi, one), pv[0].hi, add2(u0.hi, u0.hi))};
+            if (!qzero[0]) {
+                const float4 q4 = to_f4(qq[0]);
                 const V4 rq = from_f4(make_float4(rcp_approx(1.f + q4.x), rcp_approx(1.f + q4.y),
                                                   rcp_approx(1.f + q4.z), rcp_approx(1.f + q4.w)));
                 av = {mul2(av.lo, rq.lo), mul2(av.hi, rq.hi)};
             }
-            const V4 out = {fma2(lap.lo, cc[j].lo, av.lo), fma2(lap.hi, cc[j].hi, av.hi)};
+            const V4 out = {fma2(lap.lo, cc[0].lo, av.lo), fma2(lap.hi, cc[0].hi, av.hi)};
             if (x + 3 < xlim) {
                 *reinterpret_cast<ulonglong2*>(un + p) = make_ulonglong2(out.lo.v, out.hi.v);
             } else {
@@ -348,8 +356,13 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // nothing in flight at exit
 }
 
+// rows per warp a group
+__host__ __device__ constexpr int stream_rw(int) { return 2; }
+
+// three CTAs an SM with constant density (at most 85 registers), two with
+// the density's ring and cross terms
 template <int R, bool VD, int CH>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, VD ? 2 : 3)
 stencil2d_streamed(const Shot* __restrict__ shots, const TileRef* __restrict__ tiles) {
     const TileRef t = tiles[blockIdx.x];
     const Shot& S = shots[t.shot];
@@ -358,8 +371,9 @@ stencil2d_streamed(const Shot* __restrict__ shots, const TileRef* __restrict__ t
     const float *uc, *up;
     slot_ptrs(S, un, uc, up);
     const Layout L = S.L;
-    stencil2d_stream_body<R, VD, CH, 2>(reinterpret_cast<float*>(sw_batch_smem), L, un, uc, up,
-                                        S.C, S.Q, S.den, S.W, S.zb, t.tz, t.tx);
+    stencil2d_stream_body<R, VD, CH, stream_rw(CH)>(reinterpret_cast<float*>(sw_batch_smem), L,
+                                                    un, uc, up, S.C, S.Q, S.den, S.W, S.zb,
+                                                    t.tz, t.tx);
 }
 
 // ---- time-blocked 2D stencil (constant density) -----------------------------------
@@ -914,12 +928,12 @@ static void launch_group_t(bool configure, const Shot* shots, const TileRef* til
     stencil2d_batched<R, VD, TZ><<<ntiles, kThreads, bytes, st>>>(shots, tiles);
 }
 
-// streamed tiles of CH rows (ring of 2R + 32 rows, 2 rows per warp a group)
+// streamed tiles of CH rows (ring of kRing rows)
 template <int R, bool VD, int CH>
 static void launch_stream_t(bool configure, const Shot* shots, const TileRef* tiles,
                             int ntiles, cudaStream_t st) {
     constexpr int HX = (R + 3) & ~3;
-    const int bytes = (VD ? 2 : 1) * (2 * R + 2 * kWarps * 2) * (128 + 2 * HX) * 4;
+    const int bytes = (VD ? 2 : 1) * kRing * (128 + 2 * HX) * 4;
     if (configure) {
         cudaFuncSetAttribute(stencil2d_streamed<R, VD, CH>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -935,6 +949,7 @@ static void launch_group_r(bool configure, int tz, const Shot* shots, const Tile
     else if (tz == 32) launch_group_t<R, VD, 32>(configure, shots, tiles, ntiles, st);
     else if (tz == 64) launch_stream_t<R, VD, 64>(configure, shots, tiles, ntiles, st);
     else if (tz == 128) launch_stream_t<R, VD, 128>(configure, shots, tiles, ntiles, st);
+    else if (tz == 256) launch_stream_t<R, VD, 256>(configure, shots, tiles, ntiles, st);
     else launch_group_t<R, VD, 16>(configure, shots, tiles, ntiles, st);
 }
 
@@ -2006,9 +2021,10 @@ extern "C" int simwave_batch_release(simwave_batch* b, int shot_id) {
 extern "C" int simwave_batch_set_tile_rows(simwave_batch* b, int space_order, int rows) {
     return sw::batch::guarded([&] {
         if (!b || space_order < 2 || space_order > 20 || space_order % 2 ||
-            (rows != 8 && rows != 16 && rows != 32 && rows != 64 && rows != 128))
+            (rows != 8 && rows != 16 && rows != 32 && rows != 64 && rows != 128 &&
+             rows != 256))
             sw::batch::fail(SIMWAVE_E_ARGUMENT,
-                            "space_order even in 2..20, rows 8, 16, 32, 64 or 128");
+                            "space_order even in 2..20, rows 8, 16, 32, 64, 128 or 256");
         std::lock_guard<std::mutex> lock(sw::batch::g_mutex);
         Engine* e = sw::batch::engine(b);
         e->tile_rows[space_order / 2] = rows;

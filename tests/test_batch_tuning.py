@@ -31,8 +31,9 @@ def test_rows_from_each_order_and_depth_only_with_margin(monkeypatch):
         orders = {int(p.problem.space_order) for p in probs}
         if len(probs) < len(shots):  # one order alone: rows only
             (o,) = orders
-            return {8: 3.0, 16: 1.0, 32: 2.0, 64: 1.5, 128: 2.5}[tuning[o]["rows"]] \
-                if o == 4 else {8: 1.0, 16: 2.0, 32: 3.0, 64: 4.0, 128: 5.0}[tuning[o]["rows"]]
+            return {8: 3.0, 16: 1.0, 32: 2.0, 64: 1.5, 128: 2.5, 256: 2.5}[tuning[o]["rows"]] \
+                if o == 4 else {8: 1.0, 16: 2.0, 32: 3.0, 64: 4.0, 128: 5.0,
+                                256: 5.0}[tuning[o]["rows"]]
         t = 10.0
         t -= {1: 0.0, 2: 0.5, 4: 1.0}[tuning[4]["depth"]]   # 5 % and 10 % faster
         t -= {1: 0.0, 2: 0.1}[tuning[8]["depth"]]           # 1 %: below the margin

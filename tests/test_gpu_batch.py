@@ -40,7 +40,7 @@ def test_batch_matches_oracle():
         assert rel_l2(p.shot_record_numpy(), rrec) <= 1e-4
 
 
-@pytest.mark.parametrize("rows", [8, 16, 32, 64, 128])
+@pytest.mark.parametrize("rows", [8, 16, 32, 64, 128, 256])
 def test_batch_tile_heights_agree(rows):
     from simwave_gb300.batch import BatchEngine, run_batch
     from simwave_gb300.device import DeviceProblem
@@ -61,7 +61,7 @@ def test_batch_tile_heights_agree(rows):
     eng.close()
 
 
-@pytest.mark.parametrize("rows", [64, 128])
+@pytest.mark.parametrize("rows", [64, 128, 256])
 def test_streamed_tiles_bitwise_equal_staged_tiles(rows):
     """Tall tiles streamed through a ring of rows give the 16-row staged
     tiles' results bit for bit (the same per-point arithmetic), on shots of
@@ -297,7 +297,7 @@ def test_autotune_returns_a_valid_setting():
     tuning = autotune(probs, steps=16)
     assert set(tuning) == {int(k["space_order"]) for k in kws}
     for t in tuning.values():
-        assert t["rows"] in (8, 16, 32, 64, 128) and 1 <= t["depth"] <= 4
+        assert t["rows"] in (8, 16, 32, 64, 128, 256) and 1 <= t["depth"] <= 4
     eng = BatchEngine()
     eng.apply(tuning)
     run_batch(probs, engine=eng)
