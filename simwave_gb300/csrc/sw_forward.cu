@@ -5,6 +5,7 @@
 // error reporting. Kernels live in sw_kernels.cuh (generic) and
 // sw_stencil_tiled.cu (tiled fast path).
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 #include <chrono>
 #include <functional>
@@ -17,6 +18,7 @@
 #include <thread>
 #include <vector>
 
+#include <sys/mman.h>
 #include <unistd.h>
 
 #include "simwave_gb300.h"
@@ -201,11 +203,14 @@ static Arena& arena_for_current_device() {
     Arena& a = g_arenas[dev];
     if (!a.stream) SW_CUDA(cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking));
     if (!a.copy_in || !a.copy_out) {
-        // copies at the lowest priority: the time loop's blocks go first
+        // copies at the highest priority: their repack kernels are small
+        // (a read and a write of one grid) and get the next free block
+        // slots, so a snapshot leaves while the time loop runs instead of
+        // after it
         int lo = 0, hi = 0;
         SW_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-        SW_CUDA(cudaStreamCreateWithPriority(&a.copy_in, cudaStreamNonBlocking, lo));
-        SW_CUDA(cudaStreamCreateWithPriority(&a.copy_out, cudaStreamNonBlocking, lo));
+        SW_CUDA(cudaStreamCreateWithPriority(&a.copy_in, cudaStreamNonBlocking, hi));
+        SW_CUDA(cudaStreamCreateWithPriority(&a.copy_out, cudaStreamNonBlocking, hi));
         int pageable = 0;
         SW_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
         a.host_access = pageable != 0;
@@ -600,11 +605,27 @@ struct HostArgs {
 // array into a dense device staging buffer, then a repack into the pitched
 // layout on the device (and the reverse), so that the host link runs at full
 // rate; two staging buffers per direction alternate.
+// SMs of the current device (cached per device)
+static int sm_count() {
+    static std::atomic<int> sms[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!sms[dev & 63]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev & 63] = std::max(v, 1);
+    }
+    return sms[dev & 63];
+}
+
 template <typename T>
 static void repack(T* dst, const T* src, const Layout& L, bool to_pitched,
                    cudaStream_t st) {
     const long long rows = L.dim == 3 ? L.nz * L.nx : L.nz;
-    repack_rows<T><<<(unsigned)std::min<long long>(rows, 65535), 256, 0, st>>>(
+    // small blocks (128 threads, at most 32 registers, no shared memory): one
+    // fits beside a block of the time loop's 3D stencil on the same SM, so a
+    // snapshot's repack runs while the loop does instead of after it
+    repack_rows<T><<<(unsigned)std::min<long long>(rows, 2LL * sm_count()), 128, 0, st>>>(
         dst, src, rows, L.nfast(), L.pitch, L.lead, to_pitched);
     SW_LAUNCHED("repack_rows");
 }
@@ -614,11 +635,20 @@ static void repack(T* dst, const T* src, const Layout& L, bool to_pitched,
 // Makes every page of [p, p + bytes) resident, from all host cores, without
 // changing its contents (each page has one byte read and written back).
 // Freshly allocated arrays (numpy.zeros) are mapped lazily; page-locking them
-// would otherwise fault and clear their pages from one thread.
+// would otherwise fault and clear their pages from one thread. The range is
+// first advised for transparent huge pages (the contents are unchanged; on
+// kernels that grant huge pages only on advice, the snapshot copies into
+// large arrays finished sooner: median host call 0.87 s against 1.06 s on
+// the 472^3 benchmark shot).
 static void fault_in(void* p, size_t bytes) {
     if (!p || bytes < ((size_t)64 << 20)) return;
     const long ps = sysconf(_SC_PAGESIZE);
     const size_t page = ps > 0 ? (size_t)ps : 4096;
+    {
+        const uintptr_t a = (reinterpret_cast<uintptr_t>(p) + page - 1) / page * page;
+        const uintptr_t e = (reinterpret_cast<uintptr_t>(p) + bytes) / page * page;
+        if (e > a) madvise(reinterpret_cast<void*>(a), e - a, MADV_HUGEPAGE);
+    }
     const unsigned n = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
     char* base = static_cast<char*>(p);
     const size_t chunk = (bytes / n + page - 1) / page * page;
@@ -800,19 +830,17 @@ static double host_forward(const HostArgs<T>& A) {
     const bool direct = !pinned && ar.host_access && g_transfer_mode == SIMWAVE_TRANSFER_DIRECT;
     T* sin[2] = {nullptr, nullptr};
     T* sout[2] = {nullptr, nullptr};
-    if (!direct && !pinned)
+    if (!direct)
         for (int b = 0; b < 2; b++) {
             sin[b] = (T*)ar.stage_in[b].ensure(dense_bytes);
             sout[b] = (T*)ar.stage_out[b].ensure(dense_bytes);
         }
-    const size_t nf = (size_t)L.nfast(), rows = dense / nf;
+    // uploads (also from page-locked arrays): one contiguous copy into a
+    // dense device buffer, then a repack into the pitched layout; pitched
+    // copies move one short row per descriptor (about 20 GB/s here against
+    // about 200 GB/s for one contiguous copy)
     auto upload_grid = [&](T* dst, const T* src) {
         h2d += dense_bytes;
-        if (pinned) {
-            SW_CUDA(cudaMemcpy2DAsync(dst + L.lead, L.pitch * sizeof(T), src, nf * sizeof(T),
-                                      nf * sizeof(T), rows, cudaMemcpyHostToDevice, cin));
-            return;
-        }
         if (direct) {
             repack<T>(dst, src, L, true, cin);
             return;
@@ -823,13 +851,12 @@ static double host_forward(const HostArgs<T>& A) {
         repack<T>(dst, sin[b], L, true, cin);
         SW_CUDA(cudaEventRecord(ar.event(EV_IN + b), cin));
     };
+    // downloads (also to page-locked arrays): a repack into a dense device
+    // buffer, then one contiguous copy; pitched copies of short rows (one
+    // per x row of a grid) left the host link running at a fraction of its
+    // rate, so snapshots finished up to 0.6 s after the time loop
     auto download_grid = [&](T* dst, const T* src) {
         d2h += dense_bytes;
-        if (pinned) {
-            SW_CUDA(cudaMemcpy2DAsync(dst, nf * sizeof(T), src + L.lead, L.pitch * sizeof(T),
-                                      nf * sizeof(T), rows, cudaMemcpyDeviceToHost, cout));
-            return;
-        }
         if (direct) {
             repack<T>(dst, src, L, false, cout);
             return;
@@ -842,7 +869,7 @@ static double host_forward(const HostArgs<T>& A) {
     };
     // with the trace: device time from the call's first upload to the first
     // step and across the time loop
-    cudaEvent_t tr_ev[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t tr_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (trace) {
         for (auto& e : tr_ev) SW_CUDA(cudaEventCreate(&e));
         SW_CUDA(cudaEventRecord(tr_ev[0], cin));
@@ -961,6 +988,11 @@ static double host_forward(const HostArgs<T>& A) {
                                 cudaMemcpyDeviceToHost, st));
         d2h += rec_rows * A.nrec * sizeof(T);
     }
+    if (trace) {
+        SW_CUDA(cudaEventRecord(tr_ev[3], st));
+        SW_CUDA(cudaEventRecord(tr_ev[4], cout));
+        SW_CUDA(cudaEventRecord(tr_ev[5], cin));
+    }
     SW_CUDA(cudaStreamSynchronize(st));
     SW_CUDA(cudaStreamSynchronize(cin));
     SW_CUDA(cudaStreamSynchronize(cout));
@@ -971,6 +1003,12 @@ static double host_forward(const HostArgs<T>& A) {
         cudaEventElapsedTime(&b, tr_ev[1], tr_ev[2]);
         std::fprintf(stderr, "simwave host entry: device: uploads start -> loop start %.3f ms, "
                              "time loop %.3f ms\n", a, b);
+        float c = 0.f, d = 0.f, e = 0.f;
+        cudaEventElapsedTime(&c, tr_ev[0], tr_ev[3]);
+        cudaEventElapsedTime(&d, tr_ev[0], tr_ev[4]);
+        cudaEventElapsedTime(&e, tr_ev[0], tr_ev[5]);
+        std::fprintf(stderr, "simwave host entry: device: from uploads start, loop stream done "
+                             "%.3f ms, copies out done %.3f ms, copies in done %.3f ms\n", c, d, e);
         for (auto& e : tr_ev) cudaEventDestroy(e);
     }
     pins.release();
