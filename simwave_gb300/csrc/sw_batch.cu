@@ -1627,8 +1627,8 @@ __device__ void tile_sources_edges(const Shot2D& P, float* un, long long n, int 
     const Layout& L = P.L;
     const int r = L.r;
     const int nz = (int)L.nz, nx = (int)L.nx;
-    const int z_lo = tz == 0 ? 0 : r + 16 * tz;
-    const int z_hi = tz == P.tiles_z - 1 ? nz : r + 16 * (tz + 1);
+    const int z_lo = tz == 0 ? 0 : r + 16 * tz - P.zoff;
+    const int z_hi = tz == P.tiles_z - 1 ? nz : r + 16 * (tz + 1) - P.zoff;
     const int x_lo = tx == 0 ? 0 : r + 128 * tx;
     const int x_hi = tx == P.tiles_x - 1 ? nx : r + 128 * (tx + 1);
     const float dt2 = P.dt * P.dt;
@@ -1742,7 +1742,7 @@ stencil2d_persistent(const Persist2D P) {
         // stencil tiles, then the receivers (they read u_cur only)
         for (int t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
             stencil2d_tile<R, VD, TZ>(tile, L, un, uc, up, P.C, P.Q, P.den, P.W, P.zb,
-                                      t / P.tiles_x, t % P.tiles_x);
+                                      t / P.tiles_x, t % P.tiles_x, P.zoff);
             __syncthreads();  // the tile buffer is restaged next
             if (P.fused) tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x);
         }
@@ -1791,7 +1791,7 @@ stencil2d_step(const Shot2D P, float* un, const float* uc, const float* up, long
     if ((int)blockIdx.x < P.ntiles) {
         const int t = blockIdx.x;
         stencil2d_tile<R, VD, TZ>(reinterpret_cast<float*>(sw_batch_smem), P.L, un, uc, up, P.C,
-                                  P.Q, P.den, P.W, P.zb, t / P.tiles_x, t % P.tiles_x);
+                                  P.Q, P.den, P.W, P.zb, t / P.tiles_x, t % P.tiles_x, P.zoff);
         __syncthreads();
         tile_sources_edges(P, un, n, t / P.tiles_x, t % P.tiles_x, ring);
         return;
@@ -1874,14 +1874,25 @@ bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
     S.receivers = receivers;
     for (int e = 0; e < 4; e++) S.bc[e] = bc[e];
     const int r = L.r;
-    S.tiles_x = (int)((L.nx - 2 * r + 127) / 128);
-    S.tiles_z = (int)((L.nz - 2 * r + 15) / 16);
-    S.ntiles = S.tiles_x * S.tiles_z;
+    const long long nzi = L.nz - 2 * r;
     // owner-computes sources and edges need r + 1 rows / columns in the first
-    // and last tiles (the first hold min(extent, 16 or 128))
-    const long long last_z = (L.nz - 2 * r) - 16LL * (S.tiles_z - 1);
+    // and last tiles: the 16-row tiles start zoff rows above the interior,
+    // the smallest offset that leaves both edge tiles r + 1 rows (the rows
+    // of the grid's interior are the same whatever the offset)
+    S.zoff = 0;
+    for (int o = 0; o <= 15 - (r + 1) && nzi > 16; o++) {
+        const long long last = (nzi + o) % 16;
+        if (last == 0 || last >= r + 1) {
+            S.zoff = o;
+            break;
+        }
+    }
+    S.tiles_x = (int)((L.nx - 2 * r + 127) / 128);
+    S.tiles_z = (int)((nzi + S.zoff + 15) / 16);
+    S.ntiles = S.tiles_x * S.tiles_z;
+    const long long last_z = nzi + S.zoff - 16LL * (S.tiles_z - 1);
     const long long last_x = (L.nx - 2 * r) - 128LL * (S.tiles_x - 1);
-    const long long first_z = std::min<long long>(L.nz - 2 * r, 16);
+    const long long first_z = std::min<long long>(nzi, 16 - S.zoff);
     const long long first_x = std::min<long long>(L.nx - 2 * r, 128);
     S.fused = last_z >= r + 1 && last_x >= r + 1 && first_z >= r + 1 && first_x >= r + 1;
     return true;

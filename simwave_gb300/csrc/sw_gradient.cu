@@ -268,6 +268,7 @@ struct AdjointTiles {
     int zb[4];
     int bc[4];
     int tiles_x, tiles_z;
+    int zoff;  // the 16-row tiles start zoff rows above the interior
     const long long* pts;
     const int *rowptr, *rec, *tile_ptr;
     const float* wt;
@@ -286,17 +287,18 @@ adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* 
     const Layout& L = A.L;
     if (VD)
         batch::adjoint2d_density_tile<R, 16>(reinterpret_cast<float*>(sw_grad_smem), L, num,
-                                             nu1, nu2, A.C, A.Q, A.Gz, A.Gx, A.W, A.zb, tz, tx);
+                                             nu1, nu2, A.C, A.Q, A.Gz, A.Gx, A.W, A.zb, tz, tx,
+                                             A.zoff);
     else
         batch::stencil2d_tile<R, false, 16>(reinterpret_cast<float*>(sw_grad_smem), L, num, nu1,
-                                            nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx);
+                                            nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx, A.zoff);
     __syncthreads();
     if (A.pts)
         for (int e = A.tile_ptr[t] + threadIdx.x; e < A.tile_ptr[t + 1]; e += blockDim.x)
             inject_point(num, A.C, A.pts, A.rowptr, A.rec, A.wt, g_row, e);
     __syncthreads();
     const int nz = (int)L.nz, nx = (int)L.nx;
-    const int z0 = R + 16 * tz, z1 = min(z0 + 16, nz - R);
+    const int z0 = max(R + 16 * tz - A.zoff, R), z1 = min(R + 16 * (tz + 1) - A.zoff, nz - R);
     const int x0 = R + 128 * tx, x1 = min(x0 + 128, nx - R);
     // transposed order: z edges (the columns of this tile), then x edges
     if ((tz == A.tiles_z - 1 && A.bc[1]) || (tz == 0 && A.bc[0])) {
@@ -329,10 +331,12 @@ adjoint2d_tiles(const AdjointTiles A, float* num, const float* nu1, const float*
     const int tz = t / A.tiles_x, tx = t - (t / A.tiles_x) * A.tiles_x;
     if (VD)
         batch::adjoint2d_density_tile<R, 16>(reinterpret_cast<float*>(sw_grad_smem), A.L, num,
-                                             nu1, nu2, A.C, A.Q, A.Gz, A.Gx, A.W, A.zb, tz, tx);
+                                             nu1, nu2, A.C, A.Q, A.Gz, A.Gx, A.W, A.zb, tz, tx,
+                                             A.zoff);
     else
         batch::stencil2d_tile<R, false, 16>(reinterpret_cast<float*>(sw_grad_smem), A.L, num,
-                                            nu1, nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx);
+                                            nu1, nu2, A.C, A.Q, nullptr, A.W, A.zb, tz, tx,
+                                            A.zoff);
 }
 
 template <int R, bool VD>
@@ -669,7 +673,7 @@ struct AdjointTable {
     int npts = 0;
 };
 
-static AdjointTable build_table(const HostWindows& H, size_t count, const Layout& L,
+static AdjointTable build_table(const HostWindows& H, size_t count, const Layout& L, int zoff,
                                 Scratch& mem) {
     struct Entry {
         long long p;
@@ -679,9 +683,10 @@ static AdjointTable build_table(const HostWindows& H, size_t count, const Layout
     };
     const int r = L.r;
     const int tiles_x = (int)((L.nx - 2 * r + 127) / 128);
-    const int tiles_z = (int)((L.nz - 2 * r + 15) / 16);
+    const int tiles_z = (int)((L.nz - 2 * r + zoff + 15) / 16);
     auto tile_of = [&](long long z, long long x) {
-        const long long tz = std::min<long long>(std::max<long long>(z - r, 0) / 16, tiles_z - 1);
+        const long long tz =
+            std::min<long long>(std::max<long long>(z - r + zoff, 0) / 16, tiles_z - 1);
         const long long tx = std::min<long long>(std::max<long long>(x - r, 0) / 128, tiles_x - 1);
         return (int)(tz * tiles_x + tx);
     };
@@ -759,7 +764,7 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
     prepare_coefficients(X, mem, aligned16(seg) && aligned16(nu));
     gradient_factor<<<1024, 256, 0, st>>>(X.vel, Kf, (long long)G, X.dt);
     GR_LAUNCHED("gradient_factor");
-    const AdjointTable T = build_table(R, P->num_receivers, X.L, mem);
+    const AdjointTable T = build_table(R, P->num_receivers, X.L, X.tiled ? X.shot.zoff : 0, mem);
     float *Gz = nullptr, *Gx = nullptr;
     if (X.vd) {
         Gz = mem.get<float>(2 * G);
@@ -787,6 +792,7 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
         }
         A.tiles_x = X.shot.tiles_x;
         A.tiles_z = X.shot.tiles_z;
+        A.zoff = X.shot.zoff;
         A.pts = T.npts ? T.pts : nullptr;
         A.rowptr = T.rowptr;
         A.rec = T.rec;

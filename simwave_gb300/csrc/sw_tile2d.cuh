@@ -15,20 +15,22 @@ constexpr int kWarps = kThreads / 32;
 // Tile: 128 x-points (32 lanes x float4) by TZ rows; u (and rho) with an R
 // halo staged in shared memory by plain 16-byte loads; each warp computes
 // TZ / 8 rows. Same arithmetic as the 3D tiled kernels: unscaled half
-// weights, per-axis 1/h^2, per-point C and Q coefficients.
+// weights, per-axis 1/h^2, per-point C and Q coefficients. The tiles start
+// `zoff` rows above the interior (the first one holds TZ - zoff rows), so
+// that the first and last tiles of a shot can both be made tall enough.
 template <int R, bool VD, int TZ>
 __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, float* un,
                                                const float* uc, const float* up,
                                                const float* C, const float* Q,
                                                const float* den, const Weights<float>& W,
-                                               const int* zb, int tz, int tx) {
+                                               const int* zb, int tz, int tx, int zoff = 0) {
     constexpr int HX = (R + 3) & ~3;
     constexpr int TW = 128 + 2 * HX;   // floats per tile row
     constexpr int TH = TZ + 2 * R;     // tile rows
     constexpr int NF = VD ? 2 : 1;
     constexpr int NC = (4 + 2 * HX) / 4;             // 16-byte chunks of an x window
     constexpr int RPW = (TZ + kWarps - 1) / kWarps;  // rows per warp
-    const int z0 = R + tz * TZ;             // first row of the tile
+    const int z0 = R + tz * TZ - zoff;      // first row of the tile
     const int x0 = R + tx * 128;            // first column (interior index)
     const int col0 = (int)L.lead + x0 - HX;  // pitched column of tile column 0
     const int pitch = (int)L.pitch;
@@ -46,7 +48,7 @@ __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, flo
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
         const int z = z0 + warp + j * kWarps;
-        const bool ok = warp + j * kWarps < TZ && z < nz - R && x < xlim;
+        const bool ok = warp + j * kWarps < TZ && z >= R && z < nz - R && x < xlim;
         const long long p = (long long)z * pitch + L.lead + x;
         qzero[j] = xbox && z >= zb[0] && z < zb[1];  // damping-free box
         cc[j] = ldg_v4(C + p, ok);
@@ -64,7 +66,7 @@ __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, flo
             const int z = z0 - R + row;
             const int col = col0 + 4 * ch;
             float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (z < nz && col + 3 < pitch)
+            if (z >= 0 && z < nz && col + 3 < pitch)
                 val = *reinterpret_cast<const float4*>(src + (long long)z * pitch + col);
             *reinterpret_cast<float4*>(dst + row * TW + 4 * ch) = val;
         }
@@ -84,7 +86,7 @@ __device__ __forceinline__ void stencil2d_tile(float* tile, const Layout& L, flo
     for (int j = 0; j < RPW; j++) {
         const int rr = warp + j * kWarps;
         const int z = z0 + rr;
-        if (rr >= TZ || z >= nz - R || x >= xlim) continue;
+        if (rr >= TZ || z < R || z >= nz - R || x >= xlim) continue;
         const float* tu = tile + (rr + R) * TW + 4 * lane;      // row z, chunk start
         const float* tr = tile + TH * TW + (rr + R) * TW + 4 * lane;
         const long long p = (long long)z * pitch + L.lead + x;
@@ -189,13 +191,13 @@ __device__ __forceinline__ void adjoint2d_density_tile(float* tile, const Layout
                                                        const float* C, const float* Q,
                                                        const float* Gz, const float* Gx,
                                                        const Weights<float>& W, const int* zb,
-                                                       int tz, int tx) {
+                                                       int tz, int tx, int zoff = 0) {
     constexpr int HX = (R + 3) & ~3;
     constexpr int TW = 128 + 2 * HX;
     constexpr int TH = TZ + 2 * R;
     constexpr int NC = (4 + 2 * HX) / 4;
     constexpr int RPW = (TZ + kWarps - 1) / kWarps;
-    const int z0 = R + tz * TZ;
+    const int z0 = R + tz * TZ - zoff;
     const int x0 = R + tx * 128;
     const int col0 = (int)L.lead + x0 - HX;
     const int pitch = (int)L.pitch;
@@ -210,7 +212,7 @@ __device__ __forceinline__ void adjoint2d_density_tile(float* tile, const Layout
 #pragma unroll
     for (int j = 0; j < RPW; j++) {
         const int z = z0 + warp + j * kWarps;
-        const bool ok = warp + j * kWarps < TZ && z < nz - R && x < xlim;
+        const bool ok = warp + j * kWarps < TZ && z >= R && z < nz - R && x < xlim;
         const long long p = (long long)z * pitch + L.lead + x;
         qzero[j] = xbox && z >= zb[0] && z < zb[1];
         cc[j] = ldg_v4(C + p, ok);
@@ -228,7 +230,7 @@ __device__ __forceinline__ void adjoint2d_density_tile(float* tile, const Layout
         const int z = z0 - R + row;
         const int col = col0 + 4 * ch;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f), gz = v, gx = v;
-        if (z < nz && col + 3 < pitch) {
+        if (z >= 0 && z < nz && col + 3 < pitch) {
             const long long o = (long long)z * pitch + col;
             v = *reinterpret_cast<const float4*>(uc + o);
             gz = __ldg(reinterpret_cast<const float4*>(Gz + o));
@@ -254,7 +256,7 @@ __device__ __forceinline__ void adjoint2d_density_tile(float* tile, const Layout
     for (int j = 0; j < RPW; j++) {
         const int rr = warp + j * kWarps;
         const int z = z0 + rr;
-        if (rr >= TZ || z >= nz - R || x >= xlim) continue;
+        if (rr >= TZ || z < R || z >= nz - R || x >= xlim) continue;
         const int o = (rr + R) * TW + 4 * lane;  // row z, chunk start
         const long long p = (long long)z * pitch + L.lead + x;
         // z axis: L on nu, fd of Gz nu

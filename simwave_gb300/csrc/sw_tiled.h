@@ -83,6 +83,7 @@ struct Shot2D {
     float* receivers;
     int bc[4];
     int tiles_x, tiles_z, ntiles;
+    int zoff;  // the 16-row tiles start zoff rows above the interior
     int fused;
 };
 
