@@ -430,6 +430,24 @@ int simwave_gradient_backward(const simwave_problem *problem, size_t interval,
                               const void *checkpoints, const void *grad_receivers,
                               void *grad_velocity, void *stream);
 
+/* Several shots of one inversion at once: `nshots` problems (an array of
+ * structs) of one layout, space order, density kind and step range, with a
+ * checkpoint buffer each (simwave_gradient_checkpoints grids each). The
+ * forward writes every shot's record and checkpoints; the reverse pass
+ * writes into `grad_velocity` the SUM over the shots of dJ_s/dv for the
+ * cotangents grad_receivers[s]. When every shot takes the one-launch step
+ * (the first and last 16-row and 128-column tiles hold r + 1 rows and
+ * columns, after the tiling offset) the shots advance in lockstep, one
+ * launch per step for all of them; otherwise one after another. The reverse
+ * pass keeps every shot's segment levels at once: (interval + 8) grids a
+ * shot. No reference counterpart. */
+int simwave_gradient_forward_shots(const simwave_problem *problems, size_t nshots,
+                                   size_t interval, void *const *checkpoints, void *stream);
+int simwave_gradient_backward_shots(const simwave_problem *problems, size_t nshots,
+                                    size_t interval, const void *const *checkpoints,
+                                    const void *const *grad_receivers, void *grad_velocity,
+                                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1803,6 +1803,56 @@ stencil2d_step(const Shot2D P, float* un, const float* uc, const float* up, long
     if ((threadIdx.x & 31) == 0) P.receivers[(n - 1) * (long long)P.rec.count + w] = sum;
 }
 
+// One time step of several 2D shots of one layout in one launch (the
+// gradient's lockstep passes): `per_shot` blocks a shot, the shot's tiles
+// (stencil, sources, edges, and its ring row when it has a ring) then, with
+// `record`, its receiver blocks. Levels i_un, i_uc, i_up of the shot's level
+// array (`G` elements each); ring row at element `ring_off`.
+template <int R, bool VD, int TZ>
+__global__ void __launch_bounds__(kThreads)
+stencil2d_step_shots(const StepShot* __restrict__ shots, int per_shot, long long G, int i_un,
+                     int i_uc, int i_up, long long n, long long ring_off, int record) {
+    const int s = blockIdx.x / per_shot, b = blockIdx.x - s * per_shot;
+    const StepShot& Q = shots[s];
+    const Shot2D& P = Q.S;
+    float* un = Q.lev + i_un * G;
+    const float* uc = Q.lev + i_uc * G;
+    const float* up = Q.lev + i_up * G;
+    if (b < P.ntiles) {
+        stencil2d_tile<R, VD, TZ>(reinterpret_cast<float*>(sw_batch_smem), P.L, un, uc, up, P.C,
+                                  P.Q, P.den, P.W, P.zb, b / P.tiles_x, b % P.tiles_x, P.zoff);
+        __syncthreads();
+        tile_sources_edges(P, un, n, b / P.tiles_x, b % P.tiles_x,
+                           Q.ring ? Q.ring + ring_off : nullptr);
+        return;
+    }
+    if (!record) return;
+    const long long w = ((long long)(b - P.ntiles) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (long long)P.rec.count) return;
+    const float sum = gather_window<float, 2>(uc, P.L, P.rec.interval + w * 4,
+                                              P.rec.values + P.rec.offsets[w], threadIdx.x & 31);
+    if ((threadIdx.x & 31) == 0) P.receivers[(n - 1) * (long long)P.rec.count + w] = sum;
+}
+
+template <int R, bool VD>
+static void step_shots_r(const StepShot* shots, int nshots, int per_shot, long long G, int i_un,
+                         int i_uc, int i_up, long long n, long long ring_off, bool record,
+                         cudaStream_t st) {
+    constexpr int TZ = 16;
+    constexpr int HX = (R + 3) & ~3;
+    const int bytes = (VD ? 2 : 1) * (TZ + 2 * R) * (128 + 2 * HX) * 4;
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
+    int dev = 0;
+    SB_CUDA(cudaGetDevice(&dev));
+    if (!configured[dev & 63]) {
+        SB_CUDA(cudaFuncSetAttribute(stencil2d_step_shots<R, VD, TZ>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        configured[dev & 63] = true;
+    }
+    stencil2d_step_shots<R, VD, TZ><<<nshots * per_shot, kThreads, bytes, st>>>(
+        shots, per_shot, G, i_un, i_uc, i_up, n, ring_off, record ? 1 : 0);
+}
+
 template <int R, bool VD>
 static void step_r(const Shot2D& P, float* un, const float* uc, const float* up, long long n,
                    float* ring, cudaStream_t st) {
@@ -1851,6 +1901,20 @@ static bool persistent_r(const Persist2D& P, cudaStream_t st) {
 }
 
 }  // namespace batch
+
+void step2d_launch_shots(const StepShot* shots, int nshots, int per_shot, int r, bool vd,
+                         long long G, int i_un, int i_uc, int i_up, long long n,
+                         long long ring_off, bool record, cudaStream_t st) {
+#define SB_M(RR)                                                                             \
+    case RR:                                                                                 \
+        if (vd) batch::step_shots_r<RR, true>(shots, nshots, per_shot, G, i_un, i_uc, i_up, n, \
+                                       ring_off, record, st);                                \
+        else batch::step_shots_r<RR, false>(shots, nshots, per_shot, G, i_un, i_uc, i_up, n,  \
+                                     ring_off, record, st);                                  \
+        break;
+    switch (r) { SB_M(1) SB_M(2) SB_M(3) SB_M(4) SB_M(5) SB_M(6) SB_M(7) SB_M(8) SB_M(9) SB_M(10) }
+#undef SB_M
+}
 
 bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
                     const float* den, const float* vel, const float* damp,

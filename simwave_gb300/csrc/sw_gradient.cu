@@ -278,11 +278,11 @@ struct AdjointTiles {
 extern __shared__ __align__(16) float4 sw_grad_smem[];
 
 template <int R, bool VD>
-__global__ void __launch_bounds__(batch::kThreads)
-adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* nu2,
-               const float* g_row, const float* u_m, const float* u_m1, const float* u_m2,
-               const float* ring) {
-    const int t = blockIdx.x;
+__device__ __forceinline__ void adjoint_tile_step(const AdjointTiles& A, int t, float* num,
+                                                  const float* nu1, const float* nu2,
+                                                  const float* g_row, const float* u_m,
+                                                  const float* u_m1, const float* u_m2,
+                                                  const float* ring) {
     const int tz = t / A.tiles_x, tx = t - (t / A.tiles_x) * A.tiles_x;
     const Layout& L = A.L;
     if (VD)
@@ -320,6 +320,39 @@ adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* 
         const int i = z0 + q / w, j = x0 + q % w;
         accumulate_point(A.grad, num, u_m, u_m1, u_m2, A.K, ring, L, i, j);
     }
+}
+
+template <int R, bool VD>
+__global__ void __launch_bounds__(batch::kThreads)
+adjoint2d_step(const AdjointTiles A, float* num, const float* nu1, const float* nu2,
+               const float* g_row, const float* u_m, const float* u_m1, const float* u_m2,
+               const float* ring) {
+    adjoint_tile_step<R, VD>(A, blockIdx.x, num, nu1, nu2, g_row, u_m, u_m1, u_m2, ring);
+}
+
+// One adjoint step of several shots of one layout in one launch (the
+// lockstep reverse pass): `tiles` blocks a shot. Adjoint levels i_num,
+// i_nu1, i_nu2 of the shot's array nu, forward levels u^m, u^(m-1), u^(m-2)
+// at k + 1, k, k - 1 of its segment array, cotangent row m - 1, ring row at
+// element `ring_off`; the gradient terms go to the shot's own grid (A.grad).
+struct AdjShot {
+    AdjointTiles A;
+    float* nu;
+    const float* seg;
+    const float* g;
+    const float* ring;
+    int nrec;
+};
+
+template <int R, bool VD>
+__global__ void __launch_bounds__(batch::kThreads)
+adjoint2d_step_shots(const AdjShot* __restrict__ shots, int tiles, long long G, int i_num,
+                     int i_nu1, int i_nu2, int k, long long m, long long ring_off) {
+    const int s = blockIdx.x / tiles, t = blockIdx.x - s * tiles;
+    const AdjShot& Q = shots[s];
+    adjoint_tile_step<R, VD>(Q.A, t, Q.nu + i_num * G, Q.nu + i_nu1 * G, Q.nu + i_nu2 * G,
+                             Q.g + (m - 1) * Q.nrec, Q.seg + (k + 1) * G, Q.seg + k * G,
+                             Q.seg + (k - 1) * G, Q.ring ? Q.ring + ring_off : nullptr);
 }
 
 // Tile stencil of the adjoint alone (the separate-kernel path): nu_next
@@ -379,6 +412,51 @@ static void adjoint_launch(const AdjointTiles& A, bool fused, float* num, const 
         GR_A(1) GR_A(2) GR_A(3) GR_A(4) GR_A(5) GR_A(6) GR_A(7) GR_A(8) GR_A(9) GR_A(10)
     }
 #undef GR_A
+}
+
+template <int R, bool VD>
+static void adjoint_shots_r(const AdjShot* shots, int nshots, int tiles, long long G, int i_num,
+                            int i_nu1, int i_nu2, int k, long long m, long long ring_off,
+                            cudaStream_t st) {
+    constexpr int HX = (R + 3) & ~3;
+    const int bytes = (VD ? 3 : 1) * (16 + 2 * R) * (128 + 2 * HX) * 4;
+    static std::atomic<bool> configured[64];  // zero (false) at start; set once per device
+    int dev = 0;
+    GR_CUDA(cudaGetDevice(&dev));
+    if (!configured[dev & 63]) {
+        GR_CUDA(cudaFuncSetAttribute(adjoint2d_step_shots<R, VD>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        configured[dev & 63] = true;
+    }
+    adjoint2d_step_shots<R, VD><<<nshots * tiles, batch::kThreads, bytes, st>>>(
+        shots, tiles, G, i_num, i_nu1, i_nu2, k, m, ring_off);
+}
+
+static void adjoint_launch_shots(const AdjShot* shots, int nshots, int tiles, int r, bool vd,
+                                 long long G, int i_num, int i_nu1, int i_nu2, int k,
+                                 long long m, long long ring_off, cudaStream_t st) {
+#define GR_AS(RR)                                                                        \
+    case RR:                                                                             \
+        if (vd) adjoint_shots_r<RR, true>(shots, nshots, tiles, G, i_num, i_nu1, i_nu2, k, m, \
+                                          ring_off, st);                                 \
+        else adjoint_shots_r<RR, false>(shots, nshots, tiles, G, i_num, i_nu1, i_nu2, k, m, \
+                                        ring_off, st);                                   \
+        break;
+    switch (r) {
+        GR_AS(1) GR_AS(2) GR_AS(3) GR_AS(4) GR_AS(5) GR_AS(6) GR_AS(7) GR_AS(8) GR_AS(9) GR_AS(10)
+    }
+#undef GR_AS
+}
+
+// out += sum of the shots' gradient grids
+__global__ void sum_grids(float* __restrict__ out, const float* __restrict__ grids, int nshots,
+                          long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float acc = out[i];
+        for (int s = 0; s < nshots; s++) acc += grids[(long long)s * n + i];
+        out[i] = acc;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -861,6 +939,207 @@ static void reverse_pass(const simwave_problem* P, size_t interval, const float*
     }
 }
 
+// ---- several shots in lockstep -----------------------------------------------
+// Shots of one layout, order, density kind and step range (the shots of one
+// inversion) advance together: one launch per forward, recomputed or adjoint
+// step for all of them (their tiles one after the other), when every shot
+// takes the fused step; otherwise one shot after another.
+
+static void check_same(const std::vector<Ctx>& X) {
+    for (size_t s = 1; s < X.size(); s++) {
+        const Layout &a = X[0].L, &b = X[s].L;
+        if (a.nz != b.nz || a.nx != b.nx || a.pitch != b.pitch || a.lead != b.lead ||
+            a.r != b.r || X[s].begin != X[0].begin || X[s].end != X[0].end ||
+            X[s].vd != X[0].vd)
+            refuse(SIMWAVE_E_ARGUMENT,
+                   "shots of one call need one layout, space order, density kind and "
+                   "step range");
+    }
+}
+
+static void forward_pass_shots(const simwave_problem* P, size_t ns, size_t interval,
+                               float* const* ck, cudaStream_t st) {
+    if (interval < 1) refuse(SIMWAVE_E_ARGUMENT, "interval must be >= 1");
+    if (!P || !ck) refuse(SIMWAVE_E_ARGUMENT, "null problems or checkpoint buffers");
+    if (!ns) return;
+    std::vector<Ctx> X;
+    for (size_t s = 0; s < ns; s++) {
+        if (!ck[s]) refuse(SIMWAVE_E_ARGUMENT, "null checkpoint buffer");
+        X.push_back(make_ctx(&P[s], st, nullptr));
+    }
+    check_same(X);
+    Scratch mem(st);
+    const size_t G = (size_t)X[0].grid, bytes = G * sizeof(float);
+    float* lev = mem.get<float>(3 * G * ns);
+    GR_CUDA(cudaMemsetAsync(lev, 0, 3 * bytes * ns, st));
+    bool lockstep = true;
+    for (size_t s = 0; s < ns; s++) {
+        prepare_coefficients(X[s], mem, aligned16(lev) && G % 4 == 0);
+        lockstep = lockstep && X[s].tiled && X[s].fused;
+    }
+    if (!lockstep) {
+        for (size_t s = 0; s < ns; s++) forward_pass(&P[s], interval, ck[s], st);
+        return;
+    }
+    std::vector<StepShot> tab(ns);
+    int per_shot = 0;
+    for (size_t s = 0; s < ns; s++) {
+        tab[s] = StepShot{X[s].shot, lev + 3 * G * s, nullptr};
+        per_shot = std::max(per_shot, X[s].shot.ntiles +
+                                          (int)((X[s].shot.rec.count + batch::kWarps - 1) /
+                                                batch::kWarps));
+    }
+    StepShot* dtab = mem.get<StepShot>(ns);
+    GR_CUDA(cudaMemcpyAsync(dtab, tab.data(), ns * sizeof(StepShot), cudaMemcpyHostToDevice, st));
+    const Ctx& X0 = X[0];
+    for (size_t n = X0.begin; n <= X0.end; n++) {
+        const size_t i = n - X0.begin;
+        if (i % interval == 0)
+            for (size_t s = 0; s < ns; s++) {
+                const float* base = lev + 3 * G * s;
+                float* dst = ck[s] + 2 * (i / interval) * G;
+                GR_CUDA(cudaMemcpyAsync(dst, base + ((n + 2) % 3) * G, bytes,
+                                        cudaMemcpyDeviceToDevice, st));
+                GR_CUDA(cudaMemcpyAsync(dst + G, base + (n % 3) * G, bytes,
+                                        cudaMemcpyDeviceToDevice, st));
+            }
+        step2d_launch_shots(dtab, (int)ns, per_shot, X0.L.r, X0.vd, (long long)G,
+                            (int)((n + 1) % 3), (int)(n % 3), (int)((n + 2) % 3), (long long)n,
+                            0, true, st);
+        GR_LAUNCHED("stencil2d_step_shots");
+    }
+    // the table must outlive its copy: wait for the stream before returning
+    GR_CUDA(cudaStreamSynchronize(st));
+}
+
+static void reverse_pass_shots(const simwave_problem* P, size_t ns, size_t interval,
+                               const float* const* ck, const float* const* g, float* grad,
+                               cudaStream_t st) {
+    if (interval < 1) refuse(SIMWAVE_E_ARGUMENT, "interval must be >= 1");
+    if (!P || !ck || !grad || !g) refuse(SIMWAVE_E_ARGUMENT, "null argument");
+    if (!ns) return;
+    std::vector<Ctx> X;
+    std::vector<HostWindows> R(ns);
+    for (size_t s = 0; s < ns; s++) {
+        if (!ck[s] || (P[s].num_receivers && !g[s]))
+            refuse(SIMWAVE_E_ARGUMENT, "null checkpoint or cotangent buffer");
+        X.push_back(make_ctx(&P[s], st, &R[s]));
+    }
+    check_same(X);
+    Scratch mem(st);
+    const size_t G = (size_t)X[0].grid, bytes = G * sizeof(float);
+    const size_t steps = X[0].end - X[0].begin + 1;
+    const size_t K = std::min(interval, steps);
+    const long long ring_len = ring_length(X[0].L);
+    const bool dir = X[0].dirichlet;
+    // per shot: segment levels, adjoint levels, the gradient factor, the
+    // shot's gradient, the ring rows (Dirichlet edges)
+    float* seg = mem.get<float>((K + 2) * G * ns);
+    float* nu = mem.get<float>(3 * G * ns);
+    float* Kf = mem.get<float>(G * ns);
+    float* grads = mem.get<float>(G * ns);
+    float* ring = nullptr;
+    bool lockstep = true;
+    for (size_t s = 0; s < ns; s++) lockstep = lockstep && X[s].dirichlet == dir;
+    if (dir) ring = mem.get<float>(K * (size_t)ring_len * ns);
+    GR_CUDA(cudaMemsetAsync(seg, 0, (K + 2) * bytes * ns, st));
+    GR_CUDA(cudaMemsetAsync(nu, 0, 3 * bytes * ns, st));
+    GR_CUDA(cudaMemsetAsync(grads, 0, bytes * ns, st));
+    GR_CUDA(cudaMemsetAsync(grad, 0, bytes, st));
+    for (size_t s = 0; s < ns; s++) {
+        prepare_coefficients(X[s], mem, aligned16(seg) && aligned16(nu) && G % 4 == 0);
+        lockstep = lockstep && X[s].tiled && X[s].fused;
+    }
+    if (!lockstep) {
+        for (size_t s = 0; s < ns; s++) {
+            reverse_pass(&P[s], interval, ck[s], g[s], grads + s * G, st);
+        }
+        sum_grids<<<1024, 256, 0, st>>>(grad, grads, (int)ns, (long long)G);
+        GR_LAUNCHED("sum_grids");
+        GR_CUDA(cudaStreamSynchronize(st));
+        return;
+    }
+    std::vector<AdjShot> adj(ns);
+    std::vector<StepShot> rec(ns);
+    const int r = X[0].L.r;
+    for (size_t s = 0; s < ns; s++) {
+        Ctx& Xs = X[s];
+        float* Ks = Kf + s * G;
+        gradient_factor<<<1024, 256, 0, st>>>(Xs.vel, Ks, (long long)G, Xs.dt);
+        GR_LAUNCHED("gradient_factor");
+        const AdjointTable T = build_table(R[s], P[s].num_receivers, Xs.L, Xs.shot.zoff, mem);
+        float *Gz = nullptr, *Gx = nullptr;
+        if (Xs.vd) {
+            Gz = mem.get<float>(2 * G);
+            Gx = Gz + G;
+            GR_CUDA(cudaMemsetAsync(Gz, 0, 2 * bytes, st));
+            const dim3 blk(32, 8, 1);
+            const dim3 grd((unsigned)((Xs.L.nx - 2 * r + 31) / 32),
+                           (unsigned)((Xs.L.nz - 2 * r + 7) / 8), 1);
+            density_terms<<<grd, blk, 0, st>>>(Xs.den, Gz, Gx, Xs.L, Xs.W);
+            GR_LAUNCHED("density_terms");
+        }
+        AdjointTiles A{};
+        A.L = Xs.L;
+        A.C = Xs.C;
+        A.Q = Xs.Q;
+        A.K = Ks;
+        A.Gz = Gz;
+        A.Gx = Gx;
+        A.W = Xs.W;
+        for (int i = 0; i < 4; i++) {
+            A.zb[i] = Xs.zero_box[i];
+            A.bc[i] = Xs.bc[i];
+        }
+        A.tiles_x = Xs.shot.tiles_x;
+        A.tiles_z = Xs.shot.tiles_z;
+        A.zoff = Xs.shot.zoff;
+        A.pts = T.npts ? T.pts : nullptr;
+        A.rowptr = T.rowptr;
+        A.rec = T.rec;
+        A.wt = T.wt;
+        A.tile_ptr = T.tile_ptr;
+        A.grad = grads + s * G;
+        float* ring_s = dir ? ring + s * K * (size_t)ring_len : nullptr;
+        adj[s] = AdjShot{A, nu + 3 * G * s, seg + (K + 2) * G * s, g[s], ring_s,
+                         (int)P[s].num_receivers};
+        rec[s] = StepShot{Xs.shot_quiet, seg + (K + 2) * G * s, ring_s};
+    }
+    AdjShot* dadj = mem.get<AdjShot>(ns);
+    StepShot* drec = mem.get<StepShot>(ns);
+    GR_CUDA(cudaMemcpyAsync(dadj, adj.data(), ns * sizeof(AdjShot), cudaMemcpyHostToDevice, st));
+    GR_CUDA(cudaMemcpyAsync(drec, rec.data(), ns * sizeof(StepShot), cudaMemcpyHostToDevice, st));
+    const int tiles = X[0].shot.ntiles;
+    const size_t b = X[0].begin, e = X[0].end;
+    const size_t nck = checkpoint_count(steps, interval);
+    for (size_t j = nck; j-- > 0;) {
+        const size_t n0 = b + j * interval;
+        const size_t n1 = std::min(n0 + interval - 1, e);
+        for (size_t s = 0; s < ns; s++)
+            GR_CUDA(cudaMemcpyAsync(seg + (K + 2) * G * s, ck[s] + 2 * j * G, 2 * bytes,
+                                    cudaMemcpyDeviceToDevice, st));
+        for (size_t n = n0; n <= n1; n++) {
+            const size_t k = n - n0;
+            step2d_launch_shots(drec, (int)ns, tiles, r, X[0].vd, (long long)G, (int)(k + 2),
+                                (int)(k + 1), (int)k, (long long)n,
+                                (long long)(k * (size_t)ring_len), false, st);
+            GR_LAUNCHED("stencil2d_step_shots");
+        }
+        for (size_t m = n1 + 1; m >= n0 + 1; m--) {
+            if (m == e + 1) continue;  // nu^(e+1) = 0: no record reads u^(e+1)
+            const size_t k = m - n0;
+            adjoint_launch_shots(dadj, (int)ns, tiles, r, X[0].vd, (long long)G, (int)(m % 3),
+                                 (int)((m + 1) % 3), (int)((m + 2) % 3), (int)k, (long long)m,
+                                 (long long)((m - 1 - n0) * (size_t)ring_len), st);
+            GR_LAUNCHED("adjoint2d_step_shots");
+        }
+    }
+    sum_grids<<<1024, 256, 0, st>>>(grad, grads, (int)ns, (long long)G);
+    GR_LAUNCHED("sum_grids");
+    // the tables must outlive their copies
+    GR_CUDA(cudaStreamSynchronize(st));
+}
+
 template <typename F>
 static int guarded(F&& f) {
     try {
@@ -905,5 +1184,28 @@ extern "C" int simwave_gradient_backward(const simwave_problem* problem, size_t 
                                static_cast<const float*>(grad_receivers),
                                static_cast<float*>(grad_velocity),
                                static_cast<cudaStream_t>(stream));
+    });
+}
+
+extern "C" int simwave_gradient_forward_shots(const simwave_problem* problems, size_t nshots,
+                                              size_t interval, void* const* checkpoints,
+                                              void* stream) {
+    return sw::grad::guarded([&] {
+        sw::grad::forward_pass_shots(problems, nshots, interval,
+                                     reinterpret_cast<float* const*>(checkpoints),
+                                     static_cast<cudaStream_t>(stream));
+    });
+}
+
+extern "C" int simwave_gradient_backward_shots(const simwave_problem* problems, size_t nshots,
+                                               size_t interval, const void* const* checkpoints,
+                                               const void* const* grad_receivers,
+                                               void* grad_velocity, void* stream) {
+    return sw::grad::guarded([&] {
+        sw::grad::reverse_pass_shots(problems, nshots, interval,
+                                     reinterpret_cast<const float* const*>(checkpoints),
+                                     reinterpret_cast<const float* const*>(grad_receivers),
+                                     static_cast<float*>(grad_velocity),
+                                     static_cast<cudaStream_t>(stream));
     });
 }

@@ -87,6 +87,23 @@ struct Shot2D {
     int fused;
 };
 
+// One shot of a multi-shot step launch (device memory): its step parameters,
+// its level array and its ring (or null).
+struct StepShot {
+    Shot2D S;
+    float* lev;
+    float* ring;
+};
+
+// A time step of `nshots` fused shots of one layout in one launch:
+// `per_shot` >= ntiles + receiver blocks (kThreads / 32 receivers a block)
+// of the shot with the most receivers. Levels i_un, i_uc, i_up of each
+// shot's level array (G elements each); with a ring, its row at element
+// `ring_off`; with `record`, the receivers of u_cur into row n - 1.
+void step2d_launch_shots(const StepShot* shots, int nshots, int per_shot, int r, bool vd,
+                         long long G, int i_un, int i_uc, int i_up, long long n,
+                         long long ring_off, bool record, cudaStream_t st);
+
 // Fills `S`; false when the layout does not suit the tiled 2D kernel.
 bool shot2d_prepare(Shot2D& S, const Layout& L, const float* C, const float* Q,
                     const float* den, const float* vel, const float* damp,

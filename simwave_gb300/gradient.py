@@ -84,17 +84,70 @@ def shot_record(velocity, problem, interval=None):
     return _ShotRecord.apply(velocity, problem, int(interval or default_interval(steps)))
 
 
-def misfit_gradient(velocity, problems, observed, interval=None, workers=4):
+def _lockstep_ok(problems):
+    p0 = problems[0]
+    q0 = p0.problem
+    return len(problems) > 1 and all(
+        p.dim == 2 and p.dtype.itemsize == 4 and tuple(p.shape) == tuple(p0.shape) and
+        p.slot == p0.slot and p.vd == p0.vd and p.device == p0.device and
+        int(p.problem.space_order) == int(q0.space_order) and
+        int(p.problem.begin_timestep) == int(q0.begin_timestep) and
+        int(p.problem.end_timestep) == int(q0.end_timestep) for p in problems)
+
+
+def _misfit_gradient_lockstep(velocity, problems, observed, interval):
+    """All shots in lockstep through ``simwave_gradient_*_shots``: one launch
+    per forward, recomputed and adjoint step for every shot at once."""
+    lib = _lib.load()
+    p0 = problems[0]
+    n = len(problems)
+    device = velocity.device
+    interval = int(interval or default_interval(p0.timesteps))
+    stream = torch.cuda.current_stream(device)
+    v = velocity.detach()
+    for p in problems:
+        p.grid_view(p.vel).copy_(v)
+    grids = ctypes.c_size_t()
+    _check(lib.simwave_gradient_checkpoints(ctypes.byref(p0.problem), ctypes.c_size_t(interval),
+                                            ctypes.byref(grids)), "checkpoint count")
+    cks = [torch.empty(grids.value * p.slot, dtype=torch.float32, device=device)
+           for p in problems]
+    arr = (type(p0.problem) * n)(*[p.problem for p in problems])
+    ckp = (ctypes.c_void_p * n)(*[c.data_ptr() for c in cks])
+    _check(lib.simwave_gradient_forward_shots(arr, ctypes.c_size_t(n), ctypes.c_size_t(interval),
+                                              ckp, ctypes.c_void_p(stream.cuda_stream)),
+           "simwave_gradient_forward_shots")
+    total = 0.0
+    res = []
+    for p, obs in zip(problems, observed):
+        obs = torch.as_tensor(obs, dtype=torch.float32, device=device)
+        r = (p.receivers[:, :p.nrec] - obs).contiguous()
+        total += float(0.5 * torch.sum(r ** 2))
+        res.append(r)
+    out = torch.empty(p0.slot, dtype=torch.float32, device=device)
+    gp = (ctypes.c_void_p * n)(*[r.data_ptr() for r in res])
+    _check(lib.simwave_gradient_backward_shots(
+        arr, ctypes.c_size_t(n), ctypes.c_size_t(interval), ckp, gp,
+        ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)),
+        "simwave_gradient_backward_shots")
+    return total, p0.grid_view(out).contiguous()
+
+
+def misfit_gradient(velocity, problems, observed, interval=None, workers=4, lockstep=True):
     """L2 misfit over shots and its velocity gradient.
 
     ``velocity``: the extended grid (float32 tensor on the device);
     ``problems``: one ``DeviceProblem`` per shot on that grid; ``observed``:
     one shot record per shot (tensor or array, same shape as the record).
-    Shots are independent: up to ``workers`` of them run at once, each from
-    its own host thread on its own CUDA stream (a shot's launches are short,
-    so one host thread alone leaves the GPU idle between them). Returns
+    Shots of one layout, order and step range (``lockstep``) advance
+    together, one launch per step for all of them. Otherwise shots are
+    independent: up to ``workers`` of them run at once, each from its own
+    host thread on its own CUDA stream (a shot's launches are short, so one
+    host thread alone leaves the GPU idle between them). Returns
     ``(misfit, gradient)`` with the gradient on the extended grid.
     """
+    if lockstep and _lockstep_ok(problems):
+        return _misfit_gradient_lockstep(velocity, problems, observed, interval)
     import concurrent.futures
     v0 = velocity.detach()
     device = v0.device
