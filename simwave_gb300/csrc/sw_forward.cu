@@ -825,6 +825,10 @@ static double host_forward(const HostArgs<T>& A) {
         pinned = pins.add(A.u, dense_bytes * A.nslots) && pins.add(A.vel, dense_bytes) &&
                  pins.add(A.damp, dense_bytes) && (!A.vd || pins.add(A.den, dense_bytes));
         if (!pinned) pins.release();
+        // the record's rows too: a pageable copy of a freshly allocated
+        // record faulted its pages in after the time loop
+        if (pinned && rec_rows && A.nrec && A.receivers)
+            pins.add(A.receivers + (A.begin - 1) * A.nrec, rec_rows * A.nrec * sizeof(T));
     }
     stamp("pinned");
     const bool direct = !pinned && ar.host_access && g_transfer_mode == SIMWAVE_TRANSFER_DIRECT;
