@@ -180,7 +180,9 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // least 2R + 2G, so a row's slot is one AND; G = 8 RW rows a group, RW rows
 // per warp), one group ahead of the rows being computed, so each row is
 // staged once per strip (plus the 2R rows where chunks meet) instead of
-// once per overlapping 16-row tile. Per group: a CTA barrier (the
+// once per overlapping 16-row tile. A warp computes two consecutive rows of
+// a group, so they share their z neighbours (2R + 2 ring loads for the
+// pair). Per group: a CTA barrier (the
 // ring slots of the next group are free), the copies of the next group's
 // rows, a wait for the current group's, a barrier, then each warp computes
 // RW rows with the per-point arithmetic of stencil2d_tile, so the results
@@ -237,121 +239,136 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
     const P2 ihx = pk(W.ih2[1], W.ih2[1]), ihz = pk(W.ih2[0], W.ih2[0]);
     const P2 one = pk(1.f, 1.f);
 
-    // per-point operands of row z, fetched one of this warp's rows ahead
-    V4 ncc, npv, nqq;
-    bool nqz = true;
-    auto fetch = [&](int z) {
-        const bool ok = z < zend && x < xlim;
+    auto row = [&](int zz) { return ring + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
+    auto rrow = [&](int zz) { return rr + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
+    // x axis, combine, update and store of row z from its z sums
+    auto finish = [&](int z, V4 u0, V4 sz, V4 gz, V4 rz, V4 cc, V4 pv, V4 qq, bool qzero) {
+        const float* tu = row(z);
+        const float* tr = rrow(z);
         const long long p = (long long)z * pitch + L.lead + x;
-        nqz = xbox && z >= zb[0] && z < zb[1];
-        ncc = ldg_v4(C + p, ok);
-        npv = ld_v4(up + p, ok);
-        nqq = ldg_v4(Q + p, ok && !nqz);
-    };
-
-    stage(zbeg - R, zbeg + G + R);
-    fetch(zbeg + warp);
-    for (int zr = zbeg; zr < zend; zr += G) {
-        __syncthreads();  // the previous group's rows are read: their slots are free
-        stage(zr + G + R, zr + 2 * G + R);
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        __syncthreads();  // every thread's copies of this group's rows have landed
+        // x axis on pairs
+        V4 sx, gx, rx, rho;
+        {
+            P2 ev[2 * NC], od[2 * NC - 1];
+            YWindow<NC>::load(tu, ev, od);
+            P2 sh[2], gh[2];
 #pragma unroll
-        for (int j = 0; j < RW; j++) {
-            const int z = zr + warp + j * kWarps;
-            V4 cc[1] = {ncc}, pv[1] = {npv}, qq[1] = {nqq};
-            const bool qzero[1] = {nqz};
-            // the next row of this warp (the next group's first, after the last)
-            fetch(z + kWarps);
-            if (z >= zend || x >= xlim) continue;
-            auto row = [&](int zz) { return ring + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
-            auto rrow = [&](int zz) { return rr + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
-            const float* tu = row(z);
-            const float* tr = rrow(z);
-            const long long p = (long long)z * pitch + L.lead + x;
-            // z axis: rows z +- k of the ring, this lane's 4 columns
-            const V4 u0 = lds_v4(tu + HX);
-            V4 sz = vmul(w2[0], u0), gz, rz;
+            for (int h = 0; h < 2; h++) {
+                sh[h] = mul2(w2[0], h ? u0.hi : u0.lo);
 #pragma unroll
-            for (int k = 1; k <= R; k++) {
-                const V4 a = lds_v4(row(z + k) + HX);
-                const V4 b = lds_v4(row(z - k) + HX);
-                sz = vfma(w2[k], vadd(a, b), sz);
-                if (VD) {
-                    gz = k == 1 ? vmul(w1[k], vsub(a, b)) : vfma(w1[k], vsub(a, b), gz);
-                    const V4 ra = lds_v4(rrow(z + k) + HX);
-                    const V4 rb = lds_v4(rrow(z - k) + HX);
-                    rz = k == 1 ? vmul(w1[k], vsub(ra, rb)) : vfma(w1[k], vsub(ra, rb), rz);
+                for (int k = 1; k <= R; k++) {
+                    const P2 a = YWindow<NC>::at(ev, od, HX + 2 * h + k);
+                    const P2 b = YWindow<NC>::at(ev, od, HX + 2 * h - k);
+                    sh[h] = fma2(w2[k], add2(a, b), sh[h]);
+                    if (VD)
+                        gh[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), gh[h]);
                 }
             }
-            // x axis on pairs
-            V4 sx, gx, rx, rho;
-            {
-                P2 ev[2 * NC], od[2 * NC - 1];
-                YWindow<NC>::load(tu, ev, od);
-                P2 sh[2], gh[2];
+            sx = {sh[0], sh[1]};
+            gx = {gh[0], gh[1]};
+            if (VD) {
+                YWindow<NC>::load(tr, ev, od);
+                rho = {ev[HX / 2], ev[HX / 2 + 1]};
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
-                    sh[h] = mul2(w2[0], h ? u0.hi : u0.lo);
 #pragma unroll
                     for (int k = 1; k <= R; k++) {
                         const P2 a = YWindow<NC>::at(ev, od, HX + 2 * h + k);
                         const P2 b = YWindow<NC>::at(ev, od, HX + 2 * h - k);
-                        sh[h] = fma2(w2[k], add2(a, b), sh[h]);
-                        if (VD)
-                            gh[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), gh[h]);
+                        gh[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), gh[h]);
                     }
                 }
-                sx = {sh[0], sh[1]};
-                gx = {gh[0], gh[1]};
-                if (VD) {
-                    YWindow<NC>::load(tr, ev, od);
-                    rho = {ev[HX / 2], ev[HX / 2 + 1]};
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-#pragma unroll
-                        for (int k = 1; k <= R; k++) {
-                            const P2 a = YWindow<NC>::at(ev, od, HX + 2 * h + k);
-                            const P2 b = YWindow<NC>::at(ev, od, HX + 2 * h - k);
-                            gh[h] = k == 1 ? mul2(w1[k], sub2(a, b)) : fma2(w1[k], sub2(a, b), gh[h]);
-                        }
-                    }
-                    rx = {gh[0], gh[1]};
-                }
-            }
-            // reference order: x then z (constant_density/2d/wave.c:166)
-            V4 lap = vfma(ihz, sz, vmul(ihx, sx));
-            if (VD) {
-                const P2 s1x = pk(W.s1[1], W.s1[1]), s1z = pk(W.s1[0], W.s1[0]);
-                V4 cross = {mul2(s1x, mul2(gx.lo, rx.lo)), mul2(s1x, mul2(gx.hi, rx.hi))};
-                cross = {fma2(s1z, mul2(gz.lo, rz.lo), cross.lo),
-                         fma2(s1z, mul2(gz.hi, rz.hi), cross.hi)};
-                const float4 rr4 = to_f4(rho);
-                const V4 inv = from_f4(make_float4(rcp_approx(rr4.x), rcp_approx(rr4.y),
-                                                   rcp_approx(rr4.z), rcp_approx(rr4.w)));
-                lap = {fma2(sub2({0ull}, cross.lo), inv.lo, lap.lo),
-                       fma2(sub2({0ull}, cross.hi), inv.hi, lap.hi)};
-            }
-            // a = 2 u - (1 - q) u_prev;  b = a / (1 + q);  u_next = b + C lap
-            V4 av = {fma2(sub2(qq[0].lo, one), pv[0].lo, add2(u0.lo, u0.lo)),
-                     fma2(sub2(qq[0].hi, one), pv[0].hi, add2(u0.hi, u0.hi))};
-            if (!qzero[0]) {
-                const float4 q4 = to_f4(qq[0]);
-                const V4 rq = from_f4(make_float4(rcp_approx(1.f + q4.x), rcp_approx(1.f + q4.y),
-                                                  rcp_approx(1.f + q4.z), rcp_approx(1.f + q4.w)));
-                av = {mul2(av.lo, rq.lo), mul2(av.hi, rq.hi)};
-            }
-            const V4 out = {fma2(lap.lo, cc[0].lo, av.lo), fma2(lap.hi, cc[0].hi, av.hi)};
-            if (x + 3 < xlim) {
-                *reinterpret_cast<ulonglong2*>(un + p) = make_ulonglong2(out.lo.v, out.hi.v);
-            } else {
-                const float4 o = to_f4(out);
-                const float oa[4] = {o.x, o.y, o.z, o.w};
-#pragma unroll
-                for (int v = 0; v < 4; v++)
-                    if (x + v < xlim) un[p + v] = oa[v];
+                rx = {gh[0], gh[1]};
             }
         }
+        // reference order: x then z (constant_density/2d/wave.c:166)
+        V4 lap = vfma(ihz, sz, vmul(ihx, sx));
+        if (VD) {
+            const P2 s1x = pk(W.s1[1], W.s1[1]), s1z = pk(W.s1[0], W.s1[0]);
+            V4 cross = {mul2(s1x, mul2(gx.lo, rx.lo)), mul2(s1x, mul2(gx.hi, rx.hi))};
+            cross = {fma2(s1z, mul2(gz.lo, rz.lo), cross.lo),
+                     fma2(s1z, mul2(gz.hi, rz.hi), cross.hi)};
+            const float4 rr4 = to_f4(rho);
+            const V4 inv = from_f4(make_float4(rcp_approx(rr4.x), rcp_approx(rr4.y),
+                                               rcp_approx(rr4.z), rcp_approx(rr4.w)));
+            lap = {fma2(sub2({0ull}, cross.lo), inv.lo, lap.lo),
+                   fma2(sub2({0ull}, cross.hi), inv.hi, lap.hi)};
+        }
+        // a = 2 u - (1 - q) u_prev;  b = a / (1 + q);  u_next = b + C lap
+        V4 av = {fma2(sub2(qq.lo, one), pv.lo, add2(u0.lo, u0.lo)),
+                 fma2(sub2(qq.hi, one), pv.hi, add2(u0.hi, u0.hi))};
+        if (!qzero) {
+            const float4 q4 = to_f4(qq);
+            const V4 rq = from_f4(make_float4(rcp_approx(1.f + q4.x), rcp_approx(1.f + q4.y),
+                                              rcp_approx(1.f + q4.z), rcp_approx(1.f + q4.w)));
+            av = {mul2(av.lo, rq.lo), mul2(av.hi, rq.hi)};
+        }
+        const V4 out = {fma2(lap.lo, cc.lo, av.lo), fma2(lap.hi, cc.hi, av.hi)};
+        if (x + 3 < xlim) {
+            *reinterpret_cast<ulonglong2*>(un + p) = make_ulonglong2(out.lo.v, out.hi.v);
+        } else {
+            const float4 o = to_f4(out);
+            const float oa[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+            for (int v = 0; v < 4; v++)
+                if (x + v < xlim) un[p + v] = oa[v];
+        }
+    };
+    // per-point operands of row z
+    auto fetch = [&](int z, V4& cc, V4& pv, V4& qq, bool& qz) {
+        const bool ok = z < zend && x < xlim;
+        const long long p = (long long)z * pitch + L.lead + x;
+        qz = xbox && z >= zb[0] && z < zb[1];
+        cc = ldg_v4(C + p, ok);
+        pv = ld_v4(up + p, ok);
+        qq = ldg_v4(Q + p, ok && !qz);
+    };
+
+    stage(zbeg - R, zbeg + G + R);
+    for (int zr = zbeg; zr < zend; zr += G) {
+        // this warp's rows: za and za + 1, sharing their z neighbours
+        const int za = zr + 2 * warp;
+        V4 cca, pva, qqa, ccb, pvb, qqb;
+        bool qza, qzb;
+        fetch(za, cca, pva, qqa, qza);
+        fetch(za + 1, ccb, pvb, qqb, qzb);
+        __syncthreads();  // the previous group's rows are read: their slots are free
+        stage(zr + G + R, zr + 2 * G + R);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();  // every thread's copies of this group's rows have landed
+        if (za >= zend || x >= xlim) continue;
+        // z axis of both rows: at step k row za takes rows za + k and za - k,
+        // row za + 1 takes za + 1 + k and za + 1 - k; za + k and za + 1 - k
+        // were loaded at step k - 1 (the same sums as per row)
+        const V4 ua = lds_v4(row(za) + HX), ub = lds_v4(row(za + 1) + HX);
+        V4 sza = vmul(w2[0], ua), szb = vmul(w2[0], ub), gza, gzb, rza, rzb;
+        V4 am = ua, bp = ub;
+        V4 ram, rbp;
+        if (VD) {
+            ram = lds_v4(rrow(za) + HX);
+            rbp = lds_v4(rrow(za + 1) + HX);
+        }
+#pragma unroll
+        for (int k = 1; k <= R; k++) {
+            const V4 Ap = bp, Bm = am;
+            const V4 Am = lds_v4(row(za - k) + HX), Bp = lds_v4(row(za + 1 + k) + HX);
+            sza = vfma(w2[k], vadd(Ap, Am), sza);
+            szb = vfma(w2[k], vadd(Bp, Bm), szb);
+            if (VD) {
+                gza = k == 1 ? vmul(w1[k], vsub(Ap, Am)) : vfma(w1[k], vsub(Ap, Am), gza);
+                gzb = k == 1 ? vmul(w1[k], vsub(Bp, Bm)) : vfma(w1[k], vsub(Bp, Bm), gzb);
+                const V4 RAp = rbp, RBm = ram;
+                const V4 RAm = lds_v4(rrow(za - k) + HX), RBp = lds_v4(rrow(za + 1 + k) + HX);
+                rza = k == 1 ? vmul(w1[k], vsub(RAp, RAm)) : vfma(w1[k], vsub(RAp, RAm), rza);
+                rzb = k == 1 ? vmul(w1[k], vsub(RBp, RBm)) : vfma(w1[k], vsub(RBp, RBm), rzb);
+                ram = RAm;
+                rbp = RBp;
+            }
+            am = Am;
+            bp = Bp;
+        }
+        finish(za, ua, sza, gza, rza, cca, pva, qqa, qza);
+        if (za + 1 < zend) finish(za + 1, ub, szb, gzb, rzb, ccb, pvb, qqb, qzb);
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // nothing in flight at exit
 }
