@@ -718,10 +718,12 @@ static bool halo_is_zero(const T* g, int dim, size_t nz, size_t nx, size_t ny, s
 
 struct HostPins {
     std::vector<void*> mine;
+    cudaError_t last = cudaSuccess;  // the last registration's result
     bool add(const void* p, size_t bytes) {
         if (!p || !bytes) return true;
         fault_in(const_cast<void*>(p), bytes);
         cudaError_t e = cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault);
+        last = e;
         if (e == cudaSuccess) {
             mine.push_back(const_cast<void*>(p));
             return true;
@@ -830,7 +832,10 @@ static double host_forward(const HostArgs<T>& A) {
         if (pinned && rec_rows && A.nrec && A.receivers)
             pins.add(A.receivers + (A.begin - 1) * A.nrec, rec_rows * A.nrec * sizeof(T));
     }
-    stamp("pinned");
+    if (trace && !pinned)
+        std::fprintf(stderr, "simwave host entry: page-locking failed: %s\n",
+                     cudaGetErrorString(pins.last));
+    stamp(pinned ? "pinned" : "not pinned");
     const bool direct = !pinned && ar.host_access && g_transfer_mode == SIMWAVE_TRANSFER_DIRECT;
     T* sin[2] = {nullptr, nullptr};
     T* sout[2] = {nullptr, nullptr};
