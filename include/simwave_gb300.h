@@ -281,10 +281,11 @@ int simwave_forward_device(const simwave_problem *problem, void *stream);
 int simwave_set_kernel_policy(int policy);
 
 /* How the host-pointer entries move grids (process-wide).
- * AUTO: page-lock the caller's grids for the duration of the call and copy
- *   them with asynchronous pitched DMA (falls back to STAGED if locking
- *   fails); STAGED: one contiguous pageable copy per grid through a device
- *   staging buffer, repacked on the device; DIRECT: kernels read and write
+ * AUTO: page-lock the caller's grids (and the record's rows) for the
+ *   duration of the call, then copy as STAGED, asynchronously (STAGED
+ *   from pageable memory if locking fails); STAGED: one contiguous copy per
+ *   grid through a dense device staging buffer, repacked on the device
+ *   into or out of the pitched layout; DIRECT: kernels read and write
  *   the caller's pageable arrays (devices with pageable-memory access only,
  *   else STAGED). Grid snapshots leave while the time loop is still running.
  * No reference counterpart. */

@@ -805,13 +805,11 @@ static double host_forward(const HostArgs<T>& A) {
     SW_CUDA(cudaEventRecord(ar.event(EV_OUT), cout));
     SW_CUDA(cudaEventRecord(ar.event(EV_OUT + 1), cout));
     int in_turn = 0, out_turn = 0;
-    // with pageable-memory access the repack kernel reads/writes the host
-    // arrays itself (asynchronous, no staging); otherwise one contiguous
-    // copy per grid through the staging buffers
-    // transfer mode: pin the caller's grids in place for the call and let
-    // the copy engines move them with pitched DMA (AUTO), or let kernels
-    // address the pageable arrays directly (DIRECT, coherent host links), or
-    // one contiguous copy per grid through device staging (STAGED)
+    // transfer mode: AUTO page-locks the caller's grids for the call; AUTO
+    // and STAGED move each grid as one contiguous copy through a dense
+    // device staging buffer plus a repack kernel (pitched <-> dense); DIRECT
+    // (coherent host links, pageable arrays) lets the repack kernel read and
+    // write the host arrays itself, with no staging
     // SIMWAVE_TRACE set: phase times of this call on stderr
     const bool trace = std::getenv("SIMWAVE_TRACE") != nullptr;
     auto stamp = [&](const char* what) {
