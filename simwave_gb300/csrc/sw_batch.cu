@@ -241,10 +241,10 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
 
     auto row = [&](int zz) { return ring + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
     auto rrow = [&](int zz) { return rr + (int)((unsigned)zz & (NR - 1)) * TW + 4 * lane; };
-    // x axis, combine, update and store of row z from its z sums
-    auto finish = [&](int z, V4 u0, V4 sz, V4 gz, V4 rz, V4 cc, V4 pv, V4 qq, bool qzero) {
-        const float* tu = row(z);
-        const float* tr = rrow(z);
+    // x axis, combine, update and store of row z from its z sums; tu / tr:
+    // the row's lane window in the u / density ring
+    auto finish = [&](int z, const float* tu, const float* tr, V4 u0, V4 sz, V4 gz, V4 rz, V4 cc,
+                      V4 pv, V4 qq, bool qzero) {
         const long long p = (long long)z * pitch + L.lead + x;
         // x axis on pairs
         V4 sx, gx, rx, rho;
@@ -339,36 +339,64 @@ __device__ __forceinline__ void stencil2d_stream_body(float* ring, const Layout&
         if (za >= zend || x >= xlim) continue;
         // z axis of both rows: at step k row za takes rows za + k and za - k,
         // row za + 1 takes za + 1 + k and za + 1 - k; za + k and za + 1 - k
-        // were loaded at step k - 1 (the same sums as per row)
-        const V4 ua = lds_v4(row(za) + HX), ub = lds_v4(row(za + 1) + HX);
-        V4 sza = vmul(w2[0], ua), szb = vmul(w2[0], ub), gza, gzb, rza, rzb;
-        V4 am = ua, bp = ub;
-        V4 ram, rbp;
-        if (VD) {
-            ram = lds_v4(rrow(za) + HX);
-            rbp = lds_v4(rrow(za + 1) + HX);
-        }
-#pragma unroll
-        for (int k = 1; k <= R; k++) {
-            const V4 Ap = bp, Bm = am;
-            const V4 Am = lds_v4(row(za - k) + HX), Bp = lds_v4(row(za + 1 + k) + HX);
-            sza = vfma(w2[k], vadd(Ap, Am), sza);
-            szb = vfma(w2[k], vadd(Bp, Bm), szb);
+        // were loaded at step k - 1 (the same sums as per row). at(j) / rat(j):
+        // row za + j of the u / density ring (+ HX)
+        V4 ua, ub, sza, szb, gza, gzb, rza, rzb;
+        auto zsums = [&](auto at, auto rat) {
+            ua = lds_v4(at(0));
+            ub = lds_v4(at(1));
+            sza = vmul(w2[0], ua);
+            szb = vmul(w2[0], ub);
+            V4 am = ua, bp = ub;
+            V4 ram, rbp;
             if (VD) {
-                gza = k == 1 ? vmul(w1[k], vsub(Ap, Am)) : vfma(w1[k], vsub(Ap, Am), gza);
-                gzb = k == 1 ? vmul(w1[k], vsub(Bp, Bm)) : vfma(w1[k], vsub(Bp, Bm), gzb);
-                const V4 RAp = rbp, RBm = ram;
-                const V4 RAm = lds_v4(rrow(za - k) + HX), RBp = lds_v4(rrow(za + 1 + k) + HX);
-                rza = k == 1 ? vmul(w1[k], vsub(RAp, RAm)) : vfma(w1[k], vsub(RAp, RAm), rza);
-                rzb = k == 1 ? vmul(w1[k], vsub(RBp, RBm)) : vfma(w1[k], vsub(RBp, RBm), rzb);
-                ram = RAm;
-                rbp = RBp;
+                ram = lds_v4(rat(0));
+                rbp = lds_v4(rat(1));
             }
-            am = Am;
-            bp = Bp;
+#pragma unroll
+            for (int k = 1; k <= R; k++) {
+                const V4 Ap = bp, Bm = am;
+                const V4 Am = lds_v4(at(-k)), Bp = lds_v4(at(1 + k));
+                sza = vfma(w2[k], vadd(Ap, Am), sza);
+                szb = vfma(w2[k], vadd(Bp, Bm), szb);
+                if (VD) {
+                    gza = k == 1 ? vmul(w1[k], vsub(Ap, Am)) : vfma(w1[k], vsub(Ap, Am), gza);
+                    gzb = k == 1 ? vmul(w1[k], vsub(Bp, Bm)) : vfma(w1[k], vsub(Bp, Bm), gzb);
+                    const V4 RAp = rbp, RBm = ram;
+                    const V4 RAm = lds_v4(rat(-k)), RBp = lds_v4(rat(1 + k));
+                    rza = k == 1 ? vmul(w1[k], vsub(RAp, RAm)) : vfma(w1[k], vsub(RAp, RAm), rza);
+                    rzb = k == 1 ? vmul(w1[k], vsub(RBp, RBm)) : vfma(w1[k], vsub(RBp, RBm), rzb);
+                    ram = RAm;
+                    rbp = RBp;
+                }
+                am = Am;
+                bp = Bp;
+            }
+        };
+        // the pair's rows za - R .. za + 1 + R: when their slots do not wrap
+        // around the ring's end (the same for the whole warp), one base
+        // address and constant offsets; else a slot per row
+        const int s0 = (int)((unsigned)(za - R) & (NR - 1));
+        const float *tua, *tub, *tra, *trb;
+        if (s0 + 2 * R + 1 < NR) {
+            const float* wb = ring + s0 * TW + 4 * lane;
+            const float* wr = rr + s0 * TW + 4 * lane;
+            zsums([&](int j) { return wb + (R + j) * TW + HX; },
+                  [&](int j) { return wr + (R + j) * TW + HX; });
+            tua = wb + R * TW;
+            tub = wb + (R + 1) * TW;
+            tra = wr + R * TW;
+            trb = wr + (R + 1) * TW;
+        } else {
+            zsums([&](int j) { return row(za + j) + HX; },
+                  [&](int j) { return rrow(za + j) + HX; });
+            tua = row(za);
+            tub = row(za + 1);
+            tra = rrow(za);
+            trb = rrow(za + 1);
         }
-        finish(za, ua, sza, gza, rza, cca, pva, qqa, qza);
-        if (za + 1 < zend) finish(za + 1, ub, szb, gzb, rzb, ccb, pvb, qqb, qzb);
+        finish(za, tua, tra, ua, sza, gza, rza, cca, pva, qqa, qza);
+        if (za + 1 < zend) finish(za + 1, tub, trb, ub, szb, gzb, rzb, ccb, pvb, qqb, qzb);
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // nothing in flight at exit
 }
