@@ -1,9 +1,11 @@
 """Model known answers: the expected values of the reference's
 tests/test_space_model.py (defaults, shapes, extended shapes with damping
 layers and halos, layer widths in points, FD weights, halo sizes, boundary
-configuration, padded array shapes) and of tests/test_time_model.py:8-31
-(TimeModel properties), checked on this package's front end. The time-step
-counts with stride padding are in test_frontend.py. CPU only."""
+configuration, padded array shapes), of tests/test_time_model.py:8-31
+(TimeModel properties) and of tests/test_source.py:8-116 (Source
+properties, grid positions, positions on the extended grid), checked on this
+package's front end. The time-step counts with stride padding and the KWS
+interpolation points and values are in test_frontend.py. CPU only."""
 import numpy as np
 import pytest
 
@@ -149,3 +151,43 @@ def test_time_model_properties():
     assert tm.space_model == sm
     assert (tm.tf, tm.t0, tm.saving_stride) == (1.0, 0.0, 1)
     assert tm.dt == sm.dtype(0.001)
+
+
+@pytest.mark.parametrize("dim, coords", [
+    (2, [(0, 25)]), (2, [(0, 25), [250, 250]]), (3, [(0.5, 50.8, 500)]),
+])
+def test_source_properties(dim, coords):
+    # tests/test_source.py:8-43
+    sm = _model(dim, (0, 500) * dim)
+    src = sw.Source(sm, coordinates=coords, window_radius=8)
+    assert src.space_model == sm
+    assert (src.window_radius, src.count) == (8, len(coords))
+    assert np.array_equal(src.coordinates, sm.dtype(coords))
+
+
+@pytest.mark.parametrize("bbox, spacing, coords, positions", [
+    ((0, 5120, 0, 5120), (10, 10), (0, 512), (0, 51.2)),
+    ((0, 5120, 0, 5120), (10, 5), (120, 500), (12, 100)),
+    ((0, 500, 20, 500, 0, 200), (20, 20, 20), (10, 20, 100), (0.5, 0.0, 5.0)),
+])
+def test_source_grid_positions(bbox, spacing, coords, positions):
+    # tests/test_source.py:45-76: coordinates in grid units from the box origin
+    sm = _model(len(spacing), bbox, spacing)
+    src = sw.Source(sm, coordinates=coords, window_radius=4)
+    assert np.array_equal(src.grid_positions, np.asarray([positions], dtype=sm.dtype))
+
+
+@pytest.mark.parametrize("dim, length, order, coords, positions", [
+    (2, 500, 2, (0, 0), [(51, 51)]),
+    (2, 0, 2, (0, 0), [(1, 1)]),
+    (2, 0, 4, (250, 100), [(27, 12)]),
+    (2, 50, 16, (255, 255), [(38.5, 38.5)]),
+    (3, (50, 0, 50, 0, 0, 0), 16, (255, 255, 0), [(38.5, 38.5, 8)]),
+    (3, 2, 4, (250, 100, 100), [(27, 12, 12)]),
+])
+def test_source_positions_on_the_extended_grid(dim, length, order, coords, positions):
+    # tests/test_source.py:78-116: shifted by the layer and the halo
+    sm = _model(dim, (0, 500) * dim, order=order)
+    sm.config_boundary(damping_length=length)
+    src = sw.Source(sm, coordinates=coords)
+    assert np.array_equal(src.adjusted_grid_positions, sm.dtype(positions))
