@@ -55,8 +55,6 @@ namespace sw {
 
 namespace {
 
-constexpr int kTmStages = 3;  // planes in flight per field
-
 __host__ __device__ constexpr int pow2_at_least(int n) {
     int p = 32;
     while (p < n) p *= 2;
